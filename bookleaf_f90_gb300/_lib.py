@@ -1,0 +1,60 @@
+"""Loader of the in-tree CUDA library (libbookleaf_gb300.so).
+
+There is no CPU fallback: importing works anywhere, but ``load()`` raises
+if the library is missing or cannot be loaded, and ``bl_init`` itself fails
+when no CUDA device is present.
+"""
+import ctypes as ct
+import os
+
+from . import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_lib", "libbookleaf_gb300.so")
+
+_lib = None
+
+
+def load(build_if_missing=True):
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB):
+        if not build_if_missing:
+            raise RuntimeError("libbookleaf_gb300.so is not built (run __graft_entry__.build())")
+        from . import build
+        build.build()
+    L = ct.CDLL(LIB)
+    P = ct.POINTER
+    vp = ct.c_void_p
+    L.bl_init.argtypes = [P(vp), P(abi.Sizes), P(abi.Config), vp, ct.c_int, P(abi.Error)]
+    L.bl_init.restype = ct.c_int
+    L.bl_finalize.argtypes = [vp]
+    L.bl_finalize.restype = ct.c_int
+    for nm in ("bl_getdt", "bl_lagstep", "bl_alestep"):
+        f = getattr(L, nm)
+        f.argtypes = [vp, P(abi.Timestep), P(abi.Error)]
+        f.restype = ct.c_int
+    L.bl_run.argtypes = [vp, P(abi.Timestep), ct.c_int, vp, P(ct.c_int), P(abi.Error)]
+    L.bl_run.restype = ct.c_int
+    L.bl_sync_to_host.argtypes = [vp, ct.c_int]
+    L.bl_sync_to_host.restype = ct.c_int
+    L.bl_sync_to_device.argtypes = [vp, ct.c_int]
+    L.bl_sync_to_device.restype = ct.c_int
+    L.bl_synchronize.argtypes = [vp]
+    L.bl_synchronize.restype = ct.c_int
+    L.bl_stream.argtypes = [vp]
+    L.bl_stream.restype = vp
+    L.bl_kernel_launches.argtypes = [vp]
+    L.bl_kernel_launches.restype = ct.c_longlong
+    L.bl_version.restype = ct.c_char_p
+    L.bl_abi_sizes.argtypes = [P(ct.c_int), ct.c_int]
+    L.bl_abi_sizes.restype = ct.c_int
+    _lib = L
+    return L
+
+
+# Every exported entry point include/bookleaf_gb300.h declares.
+EXPORTS = ("bl_init", "bl_finalize", "bl_getdt", "bl_lagstep", "bl_alestep", "bl_run",
+           "bl_sync_to_host", "bl_sync_to_device", "bl_synchronize", "bl_stream",
+           "bl_kernel_launches", "bl_version")

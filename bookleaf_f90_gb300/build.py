@@ -1,0 +1,74 @@
+"""Build the sm_103a shared library libbookleaf_gb300.so in-tree.
+
+Three translation units, compiled in parallel with nvcc:
+  bl_kernels.cu  -DBL_NS=fast  --fmad=true   (fused multiply-add allowed)
+  bl_kernels.cu  -DBL_NS=exact --fmad=false  (bit-reproducible path)
+  bl_capi.cu                                  (the C-ABI, host code)
+and linked with the CUDA runtime statically, so the library needs nothing
+but the driver at run time.
+"""
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUTDIR = os.path.join(HERE, "_lib")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(OUTDIR, "libbookleaf_gb300.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+HEADERS = ["bl_device.cuh", "bl_kernels.h", "hydro_kernels.cuh", "ale_kernels.cuh"]
+
+
+def nvcc():
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the GB300 library cannot be built")
+
+
+def _sources():
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    deps.append(os.path.join(HERE, "..", "include", "bookleaf_gb300.h"))
+    return deps
+
+
+def build(force=False, verbose=False, extra=()):
+    os.makedirs(OUTDIR, exist_ok=True)
+    os.makedirs(BUILD, exist_ok=True)
+    newest = max(os.path.getmtime(p) for p in _sources())
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
+        return LIB
+    cc = nvcc()
+    common = [cc] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                            "-Xptxas", "-v" if verbose else "-O3"] + list(extra)
+    jobs = [
+        (common + ["--fmad=true", "-DBL_NS=fast", "-c", os.path.join(CSRC, "bl_kernels.cu"),
+                   "-o", os.path.join(BUILD, "k_fast.o")]),
+        (common + ["--fmad=false", "-DBL_NS=exact", "-c", os.path.join(CSRC, "bl_kernels.cu"),
+                   "-o", os.path.join(BUILD, "k_exact.o")]),
+        (common + ["-c", os.path.join(CSRC, "bl_capi.cu"), "-o", os.path.join(BUILD, "capi.o")]),
+    ]
+    procs = [subprocess.Popen(j, stdout=subprocess.PIPE, stderr=subprocess.STDOUT) for j in jobs]
+    logs = []
+    for j, p in zip(jobs, procs):
+        out, _ = p.communicate()
+        logs.append(out.decode(errors="replace"))
+        if p.returncode != 0:
+            sys.stderr.write(out.decode(errors="replace"))
+            raise RuntimeError("nvcc failed: " + " ".join(j))
+    tmp = LIB + ".%d.tmp" % os.getpid()
+    subprocess.check_call([cc] + ARCH + ["-shared", "-cudart", "static", "-o", tmp,
+                                         os.path.join(BUILD, "k_fast.o"),
+                                         os.path.join(BUILD, "k_exact.o"),
+                                         os.path.join(BUILD, "capi.o")])
+    os.replace(tmp, LIB)
+    if verbose:
+        sys.stdout.write("\n".join(logs))
+    return LIB
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv, verbose="-v" in sys.argv)
+    print(LIB)

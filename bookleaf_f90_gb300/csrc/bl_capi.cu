@@ -1,0 +1,905 @@
+// bl_capi.cu -- the C-ABI of include/bookleaf_gb300.h.
+//
+// Host side of the drop-in boundary: it owns the device mirrors of the
+// dataAPI fields the hot path touches, the node->corner CSR tables, the
+// device time-step state, and it sequences the kernels of bl_kernels.cu the
+// way inf_solver_getdt / inf_solver_lagstep / inf_solver_alestep sequence
+// the reference's loops.  No CPU fallback exists: every entry point fails
+// when CUDA is not usable.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "../../include/bookleaf_gb300.h"
+#include "bl_device.cuh"
+#include "bl_kernels.h"
+
+using bl::DevStep;
+using bl::d4;
+
+struct bl_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bl_sizes s{};
+  bl_config c{};
+  int fp_mode = BL_FP_FAST;
+  void* host[BL_NID + 1] = {};
+  bl::DevFields F{};
+  bl::DevCfg C{};
+  bl::Launchers L{};
+  std::vector<void*> bufs;
+  DevStep* hstep = nullptr;  // pinned mirror of F.step
+  bool cs2_is_v = false;     // elcs2 currently holds cs2 + elvisc (after getdt)
+  long long launches = 0;
+  // bl_run
+  cudaGraphExec_t gexec = nullptr;
+  int gsteps = 0;
+  bool g_ale = false;
+  int hist_cap = 0;
+  std::vector<int> ielmat_h;  // for timestep%mdt
+};
+
+namespace {
+
+const bl::Launchers kFast = {bl::fast::getdt_blocks, bl::fast::launch_getdt,
+                             bl::fast::launch_lag_force, bl::fast::launch_lag_accel,
+                             bl::fast::launch_lag_state, bl::fast::launch_ale};
+const bl::Launchers kExact = {bl::exact::getdt_blocks, bl::exact::launch_getdt,
+                              bl::exact::launch_lag_force, bl::exact::launch_lag_accel,
+                              bl::exact::launch_lag_state, bl::exact::launch_ale};
+
+void set_err(bl_error* e, int ierr, int iout, const char* msg) {
+  if (!e) return;
+  e->ierr = ierr;
+  e->iout = iout;
+  std::strncpy(e->serr, msg ? msg : "", BL_SLEN);
+  e->serr[BL_SLEN] = 0;
+}
+
+int cuda_fail(bl_error* e, cudaError_t r, const char* where) {
+  char msg[BL_SLEN + 1];
+  std::snprintf(msg, sizeof msg, "ERROR: CUDA %s in %s", cudaGetErrorString(r), where);
+  set_err(e, BL_FAILURE, BL_HALT_ALL, msg);
+  return BL_FAILURE;
+}
+
+template <class T>
+T* dalloc(bl_ctx* x, size_t n, cudaError_t& st) {
+  if (n == 0) n = 1;
+  void* p = nullptr;
+  cudaError_t r = cudaMalloc(&p, n * sizeof(T));
+  if (r != cudaSuccess) {
+    st = r;
+    return nullptr;
+  }
+  cudaMemsetAsync(p, 0, n * sizeof(T), x->stream);
+  x->bufs.push_back(p);
+  return static_cast<T*>(p);
+}
+
+template <class T>
+void up(bl_ctx* x, T* d, const void* h, size_t n) {
+  if (h && n) cudaMemcpyAsync(d, h, n * sizeof(T), cudaMemcpyHostToDevice, x->stream);
+}
+
+// Fields copied back by bl_sync_to_host(ctx, 0): the state a host reader of
+// the reference sees between solver calls.
+const int kStateIds[] = {BL_ELDENSITY, BL_ELENERGY, BL_ELPRESSURE, BL_ELCS2, BL_ELVOLUME,
+                         BL_A1, BL_A2, BL_A3, BL_B1, BL_B2, BL_B3, BL_CNWT, BL_CNX, BL_CNY,
+                         BL_CNVISCX, BL_CNVISCY, BL_ELVISC, BL_ELMASS, BL_CNMASS, BL_NDX,
+                         BL_NDY, BL_NDU, BL_NDV, BL_CPDENSITY, BL_CPENERGY, BL_CPPRESSURE,
+                         BL_CPCS2, BL_CPVOLUME, BL_CPA1, BL_CPA3, BL_CPB1, BL_CPB3};
+
+bool ale_active(const bl_config& c, double time) {  // ale_dr_utils.f90:35-51
+  if (!c.ale_zexist) return false;
+  return (time >= c.ale_mintime) && (time <= c.ale_maxtime);
+}
+
+const char* kSdt[5] = {" MAXIMUM", "  GROWTH", " INITIAL", "     CFL", "     DIV"};
+
+void fill_ts_from_step(bl_ctx* x, const DevStep& S, bl_timestep* ts) {
+  ts->nstep = S.nstep;
+  ts->dt = S.dt;
+  ts->time = S.time;
+  ts->idtel = S.idtel;
+  std::memset(ts->sdt, 0, sizeof ts->sdt);
+  std::memcpy(ts->sdt, kSdt[S.sdt < 0 || S.sdt > 4 ? 0 : S.sdt], 8);
+  std::memset(ts->mdt, 0, sizeof ts->mdt);
+  // time_dr_setmaterial (time_dr_advance.f90:134-155)
+  if (S.idtel > 0 && S.idtel <= x->s.nel) {
+    int ii = x->ielmat_h[S.idtel - 1];
+    if (ii > 0) {
+      ts->imdt = ii;
+      std::snprintf(ts->mdt, sizeof ts->mdt, "%10d", ii);
+    } else {
+      ts->imdt = 0;
+      std::memcpy(ts->mdt, "     MIXED", 10);
+    }
+  } else {
+    ts->imdt = -1;
+    std::memcpy(ts->mdt, "   UNKNOWN", 10);
+  }
+}
+
+void header_from_ts(bl_ctx* x, const bl_timestep* ts, int run_mode) {
+  DevStep& h = *x->hstep;
+  std::memset(&h, 0, sizeof h);
+  h.time = ts->time;
+  h.dt = ts->dt;
+  h.dts = ts->dts;
+  h.nstep = ts->nstep;
+  h.idtel = ts->idtel;
+  h.run_mode = run_mode;
+  cudaMemcpyAsync(x->F.step, x->hstep, sizeof(DevStep), cudaMemcpyHostToDevice, x->stream);
+}
+
+int fetch_header(bl_ctx* x, bl_error* e, const char* where) {
+  cudaMemcpyAsync(x->hstep, x->F.step, sizeof(DevStep), cudaMemcpyDeviceToHost, x->stream);
+  cudaError_t r = cudaStreamSynchronize(x->stream);
+  if (r != cudaSuccess) return cuda_fail(e, r, where);
+  r = cudaGetLastError();
+  if (r != cudaSuccess) return cuda_fail(e, r, where);
+  return BL_SUCCESS;
+}
+
+int negvol_error(int code, bl_error* e) {
+  set_err(e, -code, BL_HALT_SINGLE, "ERROR: negative volume in geometry_dr_getgeometry");
+  return -code;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* bl_version(void) { return "bookleaf_gb300 1.0 (sm_103a)"; }
+
+int bl_init(bl_ctx** out, const bl_sizes* sizes, const bl_config* config, void* const* dh,
+            int fp_mode, bl_error* error) {
+  set_err(error, BL_SUCCESS, BL_HALT_SINGLE, "");
+  if (!out || !sizes || !config || !dh) {
+    set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init: null argument");
+    return BL_FAILURE;
+  }
+  *out = nullptr;
+  int ndev = 0;
+  cudaError_t r = cudaGetDeviceCount(&ndev);
+  if (r != cudaSuccess || ndev < 1) {
+    set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: no CUDA device available for the hot path");
+    return BL_FAILURE;
+  }
+  const bl_sizes& s = *sizes;
+  const bl_config& c = *config;
+  if (s.nel < 1 || s.nnd < 4 || s.nreg < 1 || s.nreg > BL_MAXREG || s.nmat < 1 ||
+      s.nmat > BL_MAXMAT || s.ncp < 0 || s.nmx < 0) {
+    set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init: sizes out of range");
+    return BL_FAILURE;
+  }
+  if (c.ale_zexist && !c.ale_zeul) {
+    set_err(error, BL_FAILURE, BL_HALT_ALL,
+            "ERROR: ALE requires zeul (the reference implements no other mesh motion)");
+    return BL_FAILURE;
+  }
+  static const int needed[] = {BL_ELDENSITY, BL_ELENERGY, BL_ELPRESSURE, BL_ELCS2,
+                               BL_ELVOLUME, BL_A1, BL_A3, BL_B1, BL_B3, BL_CNWT, BL_ELMASS,
+                               BL_CNMASS, BL_NDX, BL_NDY, BL_NDU, BL_NDV, BL_INDTYPE,
+                               BL_IELSORT1, BL_IELND, BL_IELEL, BL_IELFC, BL_IELMAT, BL_IELREG};
+  for (int id : needed)
+    if (!dh[id]) {
+      char msg[BL_SLEN + 1];
+      std::snprintf(msg, sizeof msg, "ERROR: bl_init: field %d not registered", id);
+      set_err(error, BL_FAILURE, BL_HALT_ALL, msg);
+      return BL_FAILURE;
+    }
+  if (c.zsp && !dh[BL_SPMASS]) {
+    set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init: spmass needed (zsp)");
+    return BL_FAILURE;
+  }
+  const int nel = s.nel, nnd = s.nnd, ncp = s.ncp, nmx = s.nmx;
+  const int* ielnd = static_cast<const int*>(dh[BL_IELND]);
+  const int* ielel = static_cast<const int*>(dh[BL_IELEL]);
+  const int* ielfc = static_cast<const int*>(dh[BL_IELFC]);
+  const int* ielreg = static_cast<const int*>(dh[BL_IELREG]);
+  const int* srt1 = static_cast<const int*>(dh[BL_IELSORT1]);
+  // host-side bounds validation before anything reaches the device
+  for (long k = 0; k < 4L * nel; k++) {
+    if (ielnd[k] < 1 || ielnd[k] > nnd || ielel[k] < 1 || ielel[k] > nel || ielfc[k] < 1 ||
+        ielfc[k] > 4) {
+      set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init: connectivity out of range");
+      return BL_FAILURE;
+    }
+  }
+  for (int i = 0; i < nel; i++)
+    if (ielreg[i] < 1 || ielreg[i] > s.nreg || srt1[i] < 1 || srt1[i] > nel) {
+      set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init: ielreg/ielsort1 out of range");
+      return BL_FAILURE;
+    }
+  const int* ielmat = static_cast<const int*>(dh[BL_IELMAT]);
+  for (int i = 0; i < nel; i++)
+    if (ielmat[i] > s.nmat) {
+      set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init: ielmat out of range");
+      return BL_FAILURE;
+    }
+  if (c.ale_zexist) {
+    const int* srt2 = static_cast<const int*>(dh[BL_IELSORT2]);
+    if (!srt2) {
+      set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init: ielsort2 needed for ALE");
+      return BL_FAILURE;
+    }
+    for (int i = 0; i < nel; i++)
+      if (srt2[i] != i + 1) {
+        // serial BookLeaf sets ielsort2 to the identity (init_dr_utils.f90:65-68);
+        // ale_kn_updatend sums in natural order, calcbasisnd in ielsort2 order
+        set_err(error, BL_FAILURE, BL_HALT_ALL,
+                "ERROR: bl_init: ielsort2 must be the identity for one partition");
+        return BL_FAILURE;
+      }
+  }
+  std::vector<int> elmx(nel, -1);
+  if (ncp > 0) {
+    const int* imxel = static_cast<const int*>(dh[BL_IMXEL]);
+    const int* imxfcp = static_cast<const int*>(dh[BL_IMXFCP]);
+    const int* imxncp = static_cast<const int*>(dh[BL_IMXNCP]);
+    const int* icpmat = static_cast<const int*>(dh[BL_ICPMAT]);
+    static const int cpneed[] = {BL_CPDENSITY, BL_CPENERGY, BL_CPPRESSURE, BL_CPCS2, BL_CPVOLUME,
+                                 BL_FRVOLUME, BL_CPMASS, BL_FRMASS};
+    bool ok = imxel && imxfcp && imxncp && icpmat;
+    for (int id : cpneed) ok = ok && dh[id];
+    if (!ok) {
+      set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init: component fields missing");
+      return BL_FAILURE;
+    }
+    for (int m = 0; m < nmx; m++) {
+      if (imxel[m] < 1 || imxel[m] > nel || imxfcp[m] < 1 || imxncp[m] < 1 ||
+          imxfcp[m] + imxncp[m] - 1 > ncp) {
+        set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init: mixed-cell lists out of range");
+        return BL_FAILURE;
+      }
+      elmx[imxel[m] - 1] = m;
+    }
+    for (int k = 0; k < ncp; k++)
+      if (icpmat[k] < 0 || icpmat[k] > s.nmat) {
+        set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init: icpmat out of range");
+        return BL_FAILURE;
+      }
+  }
+
+  bl_ctx* x = new bl_ctx();
+  x->s = s;
+  x->c = c;
+  x->fp_mode = fp_mode;
+  x->L = (fp_mode == BL_FP_EXACT) ? kExact : kFast;
+  for (int id = 1; id <= BL_NID; id++) x->host[id] = dh[id];
+  x->ielmat_h.assign(ielmat, ielmat + nel);
+  cudaGetDevice(&x->device);
+  r = cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking);
+  if (r != cudaSuccess) {
+    delete x;
+    return cuda_fail(error, r, "bl_init");
+  }
+  cudaError_t st = cudaSuccess;
+  bl::DevFields& F = x->F;
+  F.nel = nel;
+  F.nnd = nnd;
+  F.ncp = ncp;
+  F.nmx = nmx;
+  // ---- connectivity, converted to 0-based
+  {
+    std::vector<int4> nd(nel), ee(nel);
+    std::vector<int> fc(nel), rg(nel);
+    for (int i = 0; i < nel; i++) {
+      nd[i] = make_int4(ielnd[4 * i] - 1, ielnd[4 * i + 1] - 1, ielnd[4 * i + 2] - 1,
+                        ielnd[4 * i + 3] - 1);
+      ee[i] = make_int4(ielel[4 * i] - 1, ielel[4 * i + 1] - 1, ielel[4 * i + 2] - 1,
+                        ielel[4 * i + 3] - 1);
+      fc[i] = (ielfc[4 * i] - 1) | ((ielfc[4 * i + 1] - 1) << 8) |
+              ((ielfc[4 * i + 2] - 1) << 16) | ((ielfc[4 * i + 3] - 1) << 24);
+      rg[i] = ielreg[i] - 1;
+    }
+    int4* d_nd = dalloc<int4>(x, nel, st);
+    int4* d_ee = dalloc<int4>(x, nel, st);
+    int* d_fc = dalloc<int>(x, nel, st);
+    int* d_rg = dalloc<int>(x, nel, st);
+    int* d_mt = dalloc<int>(x, nel, st);
+    int* d_it = dalloc<int>(x, nnd, st);
+    if (st != cudaSuccess) goto fail;
+    up(x, d_nd, nd.data(), nel);
+    up(x, d_ee, ee.data(), nel);
+    up(x, d_fc, fc.data(), nel);
+    up(x, d_rg, rg.data(), nel);
+    up(x, d_mt, ielmat, nel);
+    up(x, d_it, dh[BL_INDTYPE], nnd);
+    F.ielnd = d_nd;
+    F.ielel = d_ee;
+    F.ielfc = d_fc;
+    F.ielreg = d_rg;
+    F.ielmat = d_mt;
+    F.indtype = d_it;
+    cudaStreamSynchronize(x->stream);
+    // node -> corner CSR in hydro_kn_scatteracceleration's order: corner jj
+    // outer, elements in ielsort1 order inner (hydro_kn_getacceleration.f90:53-72)
+    std::vector<int> off(nnd + 1, 0), ent(4L * nel);
+    for (long k = 0; k < 4L * nel; k++) off[ielnd[k]]++;
+    for (int i = 0; i < nnd; i++) off[i + 1] += off[i];
+    std::vector<int> pos(off.begin(), off.end() - 1);
+    for (int jj = 0; jj < 4; jj++)
+      for (int kk = 0; kk < nel; kk++) {
+        const int iel = srt1[kk] - 1;
+        const int ind = ielnd[4 * iel + jj] - 1;
+        ent[pos[ind]++] = 4 * iel + jj;
+      }
+    int* d_off = dalloc<int>(x, nnd + 1, st);
+    int* d_ent = dalloc<int>(x, 4L * nel, st);
+    if (st != cudaSuccess) goto fail;
+    up(x, d_off, off.data(), nnd + 1);
+    up(x, d_ent, ent.data(), 4L * nel);
+    F.nc_off = d_off;
+    F.nc_ent = d_ent;
+    // element-major CSR (ale_kn_calcbasisnd / massbasisnd / updatend)
+    if (c.ale_zexist) {
+      std::vector<int> pos2(off.begin(), off.end() - 1), ent2(4L * nel);
+      for (int iel = 0; iel < nel; iel++)
+        for (int j = 0; j < 4; j++) {
+          const int ind = ielnd[4 * iel + j] - 1;
+          ent2[pos2[ind]++] = 4 * iel + j;
+        }
+      int* d_ent2 = dalloc<int>(x, 4L * nel, st);
+      if (st != cudaSuccess) goto fail;
+      up(x, d_ent2, ent2.data(), 4L * nel);
+      F.ne_off = d_off;
+      F.ne_ent = d_ent2;
+    }
+    cudaStreamSynchronize(x->stream);
+  }
+  // ---- node fields
+  F.ndx = dalloc<double>(x, nnd, st);
+  F.ndy = dalloc<double>(x, nnd, st);
+  F.ndu = dalloc<double>(x, nnd, st);
+  F.ndv = dalloc<double>(x, nnd, st);
+  F.ndubar = dalloc<double>(x, nnd, st);
+  F.ndvbar = dalloc<double>(x, nnd, st);
+  // ---- element fields
+  F.rho = dalloc<double>(x, nel, st);
+  F.e = dalloc<double>(x, nel, st);
+  F.p = dalloc<double>(x, nel, st);
+  F.cs2 = dalloc<double>(x, nel, st);
+  F.cs2v = dalloc<double>(x, nel, st);
+  F.vol = dalloc<double>(x, nel, st);
+  F.mass = dalloc<double>(x, nel, st);
+  F.visc = dalloc<double>(x, nel, st);
+  F.a1 = dalloc<double>(x, nel, st);
+  F.a2 = dalloc<double>(x, nel, st);
+  F.a3 = dalloc<double>(x, nel, st);
+  F.b1 = dalloc<double>(x, nel, st);
+  F.b2 = dalloc<double>(x, nel, st);
+  F.b3 = dalloc<double>(x, nel, st);
+  F.rho_h = dalloc<double>(x, nel, st);
+  F.cnwt = dalloc<d4>(x, nel, st);
+  F.cnmass = dalloc<d4>(x, nel, st);
+  F.cnviscx = dalloc<d4>(x, nel, st);
+  F.cnviscy = dalloc<d4>(x, nel, st);
+  F.cnfx = dalloc<d4>(x, nel, st);
+  F.cnfy = dalloc<d4>(x, nel, st);
+  F.cnwt_h = dalloc<d4>(x, nel, st);
+  if (c.zsp) F.spmass = dalloc<d4>(x, nel, st);
+  if (c.ale_zexist) {
+    F.fcdv = dalloc<d4>(x, nel, st);
+    F.fcdm = dalloc<d4>(x, nel, st);
+    F.eflux = dalloc<d4>(x, nel, st);
+    F.cnflux = dalloc<d4>(x, nel, st);
+    F.cnfu = dalloc<d4>(x, nel, st);
+    F.cnfv = dalloc<d4>(x, nel, st);
+    F.vpr = dalloc<double>(x, nel, st);
+    F.mpr = dalloc<double>(x, nel, st);
+    F.cutm_el = dalloc<double>(x, nel, st);
+  }
+  {
+    const int nblk = x->L.getdt_blocks(nel);
+    F.red_v = dalloc<double>(x, 2L * nblk, st);
+    F.red_i = dalloc<int>(x, 2L * nblk, st);
+  }
+  F.step = dalloc<DevStep>(x, 1, st);
+  if (st != cudaSuccess) goto fail;
+  if (cudaMallocHost(&x->hstep, sizeof(DevStep)) != cudaSuccess) {
+    st = cudaErrorMemoryAllocation;
+    goto fail;
+  }
+  std::memset(x->hstep, 0, sizeof(DevStep));
+  up(x, F.ndx, dh[BL_NDX], nnd);
+  up(x, F.ndy, dh[BL_NDY], nnd);
+  up(x, F.ndu, dh[BL_NDU], nnd);
+  up(x, F.ndv, dh[BL_NDV], nnd);
+  up(x, F.rho, dh[BL_ELDENSITY], nel);
+  up(x, F.e, dh[BL_ELENERGY], nel);
+  up(x, F.p, dh[BL_ELPRESSURE], nel);
+  up(x, F.cs2, dh[BL_ELCS2], nel);
+  up(x, F.vol, dh[BL_ELVOLUME], nel);
+  up(x, F.mass, dh[BL_ELMASS], nel);
+  up(x, F.visc, dh[BL_ELVISC], nel);
+  up(x, F.a1, dh[BL_A1], nel);
+  up(x, F.a2, dh[BL_A2], nel);
+  up(x, F.a3, dh[BL_A3], nel);
+  up(x, F.b1, dh[BL_B1], nel);
+  up(x, F.b2, dh[BL_B2], nel);
+  up(x, F.b3, dh[BL_B3], nel);
+  up(x, F.cnwt, dh[BL_CNWT], nel);
+  up(x, F.cnmass, dh[BL_CNMASS], nel);
+  up(x, F.cnviscx, dh[BL_CNVISCX], nel);
+  up(x, F.cnviscy, dh[BL_CNVISCY], nel);
+  if (c.zsp) up(x, F.spmass, dh[BL_SPMASS], nel);
+  // ---- mixed cells
+  if (ncp > 0) {
+    std::vector<int> mxel(nmx), mxf(nmx);
+    const int* imxel = static_cast<const int*>(dh[BL_IMXEL]);
+    const int* imxfcp = static_cast<const int*>(dh[BL_IMXFCP]);
+    for (int m = 0; m < nmx; m++) {
+      mxel[m] = imxel[m] - 1;
+      mxf[m] = imxfcp[m] - 1;
+    }
+    int* d_elmx = dalloc<int>(x, nel, st);
+    int* d_mxel = dalloc<int>(x, nmx, st);
+    int* d_mxf = dalloc<int>(x, nmx, st);
+    int* d_mxn = dalloc<int>(x, nmx, st);
+    int* d_cpm = dalloc<int>(x, ncp, st);
+    F.cprho = dalloc<double>(x, ncp, st);
+    F.cpe = dalloc<double>(x, ncp, st);
+    F.cpp = dalloc<double>(x, ncp, st);
+    F.cpcs2 = dalloc<double>(x, ncp, st);
+    F.cpvol = dalloc<double>(x, ncp, st);
+    F.frvol = dalloc<double>(x, ncp, st);
+    F.cpm = dalloc<double>(x, ncp, st);
+    F.frm = dalloc<double>(x, ncp, st);
+    F.cpvisc = dalloc<double>(x, ncp, st);
+    F.cpviscx = dalloc<d4>(x, ncp, st);
+    F.cpviscy = dalloc<d4>(x, ncp, st);
+    F.cpfx = dalloc<d4>(x, ncp, st);
+    F.cpfy = dalloc<d4>(x, ncp, st);
+    if (st != cudaSuccess) goto fail;
+    up(x, d_elmx, elmx.data(), nel);
+    up(x, d_mxel, mxel.data(), nmx);
+    up(x, d_mxf, mxf.data(), nmx);
+    up(x, d_mxn, dh[BL_IMXNCP], nmx);
+    up(x, d_cpm, dh[BL_ICPMAT], ncp);
+    up(x, F.cprho, dh[BL_CPDENSITY], ncp);
+    up(x, F.cpe, dh[BL_CPENERGY], ncp);
+    up(x, F.cpp, dh[BL_CPPRESSURE], ncp);
+    up(x, F.cpcs2, dh[BL_CPCS2], ncp);
+    up(x, F.cpvol, dh[BL_CPVOLUME], ncp);
+    up(x, F.frvol, dh[BL_FRVOLUME], ncp);
+    up(x, F.cpm, dh[BL_CPMASS], ncp);
+    up(x, F.frm, dh[BL_FRMASS], ncp);
+    // component viscosity is zeroed at start and never set (hydro_dr_init.f90:48-51;
+    // hydro_kn_getcpeviscosity is empty), so its device copies stay zero
+    F.elmx = d_elmx;
+    F.imxel = d_mxel;
+    F.imxfcp = d_mxf;
+    F.imxncp = d_mxn;
+    F.icpmat = d_cpm;
+    cudaStreamSynchronize(x->stream);
+  }
+  // ---- configuration tables
+  {
+    bl::DevCfg& C = x->C;
+    C.cvisc1 = c.cvisc1;
+    C.cvisc2 = c.cvisc2;
+    C.cfl_sf = c.cfl_sf;
+    C.div_sf = c.div_sf;
+    C.zcut = c.zcut;
+    C.zerocut = c.zerocut;
+    C.dencut = c.dencut;
+    C.accut = c.accut;
+    C.ccut = c.ccut;
+    C.pcut = c.pcut;
+    C.dt_g = c.dt_g;
+    C.dt_min = c.dt_min;
+    C.dt_max = c.dt_max;
+    C.dt_initial = c.dt_initial;
+    C.time_end = c.time_end;
+    C.ale_mintime = c.ale_mintime;
+    C.ale_maxtime = c.ale_maxtime;
+    C.ztq = c.ztq;
+    C.zhg = c.zhg;
+    C.zsp = c.zsp;
+    C.nreg = s.nreg;
+    C.nmat = s.nmat;
+    C.ale_zexist = c.ale_zexist;
+    C.ale_zeul = c.ale_zeul;
+    C.adv_type = c.ale_adv_type;
+    const int nr = s.nreg, nm = s.nmat + 1;
+    std::vector<double> kap(c.kappareg, c.kappareg + nr), pm(c.pmeritreg, c.pmeritreg + nr);
+    std::vector<int> zd(c.zdtnotreg, c.zdtnotreg + nr), zm(c.zmidlength, c.zmidlength + nr);
+    std::vector<int> et(c.eos_type, c.eos_type + nm);
+    std::vector<double> ep(6L * nm), gm1(nm), ggm1(nm);
+    for (int m = 0; m < nm; m++) {
+      for (int k = 0; k < 6; k++) ep[6 * m + k] = c.eos_param[m][k];
+      gm1[m] = c.eos_param[m][0] - 1.0;
+      ggm1[m] = c.eos_param[m][0] * (c.eos_param[m][0] - 1.0);
+    }
+    double* d_kap = dalloc<double>(x, nr, st);
+    double* d_pm = dalloc<double>(x, nr, st);
+    int* d_zd = dalloc<int>(x, nr, st);
+    int* d_zm = dalloc<int>(x, nr, st);
+    int* d_et = dalloc<int>(x, nm, st);
+    double* d_ep = dalloc<double>(x, 6L * nm, st);
+    double* d_g1 = dalloc<double>(x, nm, st);
+    double* d_g2 = dalloc<double>(x, nm, st);
+    if (st != cudaSuccess) goto fail;
+    up(x, d_kap, kap.data(), nr);
+    up(x, d_pm, pm.data(), nr);
+    up(x, d_zd, zd.data(), nr);
+    up(x, d_zm, zm.data(), nr);
+    up(x, d_et, et.data(), nm);
+    up(x, d_ep, ep.data(), 6L * nm);
+    up(x, d_g1, gm1.data(), nm);
+    up(x, d_g2, ggm1.data(), nm);
+    C.kappareg = d_kap;
+    C.pmeritreg = d_pm;
+    C.zdtnotreg = d_zd;
+    C.zmidlength = d_zm;
+    C.eos_type = d_et;
+    C.eos_param = d_ep;
+    C.eos_gm1 = d_g1;
+    C.eos_ggm1 = d_g2;
+    cudaStreamSynchronize(x->stream);
+  }
+  r = cudaStreamSynchronize(x->stream);
+  if (r != cudaSuccess) {
+    st = r;
+    goto fail;
+  }
+  *out = x;
+  return BL_SUCCESS;
+fail:
+  bl_finalize(x);
+  return cuda_fail(error, st == cudaSuccess ? cudaErrorMemoryAllocation : st, "bl_init");
+}
+
+int bl_finalize(bl_ctx* x) {
+  if (!x) return BL_SUCCESS;
+  if (x->stream) cudaStreamSynchronize(x->stream);
+  if (x->gexec) cudaGraphExecDestroy(x->gexec);
+  for (void* p : x->bufs) cudaFree(p);
+  if (x->F.hist) cudaFree(x->F.hist);
+  if (x->hstep) cudaFreeHost(x->hstep);
+  if (x->stream) cudaStreamDestroy(x->stream);
+  delete x;
+  return BL_SUCCESS;
+}
+
+int bl_getdt(bl_ctx* x, bl_timestep* ts, bl_error* e) {
+  set_err(e, BL_SUCCESS, BL_HALT_SINGLE, "");
+  if (!x || !ts) {
+    set_err(e, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_getdt: null argument");
+    return BL_FAILURE;
+  }
+  header_from_ts(x, ts, 0);
+  x->L.getdt(x->F, x->C, x->stream);
+  x->launches += bl::kLaunchesGetdt;
+  int rc = fetch_header(x, e, "bl_getdt");
+  if (rc != BL_SUCCESS) return rc;
+  x->cs2_is_v = true;
+  const DevStep& S = *x->hstep;
+  if (S.err_code == 1) {
+    set_err(e, BL_FAILURE, BL_HALT_SINGLE, "ERROR: negative CFL condition in hydro_dr_getdt");
+    return BL_FAILURE;
+  }
+  fill_ts_from_step(x, S, ts);
+  if (S.err_code == 2) {
+    set_err(e, BL_FAILURE, BL_HALT_ALL, "ERROR: dt < dt_min");
+    return BL_FAILURE;
+  }
+  return BL_SUCCESS;
+}
+
+int bl_lagstep(bl_ctx* x, bl_timestep* ts, bl_error* e) {
+  set_err(e, BL_SUCCESS, BL_HALT_SINGLE, "");
+  if (!x || !ts) {
+    set_err(e, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_lagstep: null argument");
+    return BL_FAILURE;
+  }
+  header_from_ts(x, ts, 0);
+  x->L.lag_force(x->F, x->C, x->stream);
+  x->L.lag_accel(x->F, x->C, x->stream);
+  x->L.lag_state(x->F, x->C, x->stream);
+  x->launches += bl::kLaunchesLagstep;
+  int rc = fetch_header(x, e, "bl_lagstep");
+  if (rc != BL_SUCCESS) return rc;
+  x->cs2_is_v = false;
+  // time_dr_setpredictor / setcorrector leave the corrector state behind
+  ts->zcorrector = 1;
+  ts->dts = ts->dt;
+  const DevStep& S = *x->hstep;
+  if (S.negvol_pred) return negvol_error(S.negvol_pred, e);
+  if (S.negvol_corr) return negvol_error(S.negvol_corr, e);
+  return BL_SUCCESS;
+}
+
+int bl_alestep(bl_ctx* x, const bl_timestep* ts, bl_error* e) {
+  set_err(e, BL_SUCCESS, BL_HALT_SINGLE, "");
+  if (!x || !ts) {
+    set_err(e, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_alestep: null argument");
+    return BL_FAILURE;
+  }
+  if (!ale_active(x->c, ts->time)) return BL_SUCCESS;
+  if (x->c.ale_adv_type != 1) {
+    set_err(e, BL_FAILURE, BL_HALT_ALL,
+            x->c.ale_adv_type == 2 ? "ERROR: adv_type 2 (split) not supported on the device"
+                                   : "ERROR: unrecognised adv_type");
+    return BL_FAILURE;
+  }
+  header_from_ts(x, ts, 0);
+  x->L.ale(x->F, x->C, x->stream);
+  x->launches += bl::kLaunchesAle;
+  int rc = fetch_header(x, e, "bl_alestep");
+  if (rc != BL_SUCCESS) return rc;
+  const DevStep& S = *x->hstep;
+  if (S.negvol_ale) return negvol_error(S.negvol_ale, e);
+  return BL_SUCCESS;
+}
+
+int bl_run(bl_ctx* x, bl_timestep* ts, int max_steps, bl_step_record* history, int* nsteps,
+           bl_error* e) {
+  set_err(e, BL_SUCCESS, BL_HALT_SINGLE, "");
+  if (nsteps) *nsteps = 0;
+  if (!x || !ts || max_steps < 0) {
+    set_err(e, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_run: bad argument");
+    return BL_FAILURE;
+  }
+  if (max_steps == 0) return BL_SUCCESS;
+  if (x->c.ale_zexist && x->c.ale_adv_type != 1) {
+    set_err(e, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_run: only adv_type 1 runs on the device");
+    return BL_FAILURE;
+  }
+  cudaError_t r;
+  if (history && max_steps > x->hist_cap) {
+    if (x->F.hist) cudaFree(x->F.hist);
+    x->F.hist = nullptr;
+    r = cudaMalloc(&x->F.hist, sizeof(bl::StepRec) * (size_t)max_steps);
+    if (r != cudaSuccess) return cuda_fail(e, r, "bl_run");
+    x->hist_cap = max_steps;
+    if (x->gexec) {  // captured with the old history pointer
+      cudaGraphExecDestroy(x->gexec);
+      x->gexec = nullptr;
+    }
+  }
+  x->C.max_records = history ? x->hist_cap : 0;
+  bl::StepRec* keep_hist = x->F.hist;
+  if (!history) x->F.hist = nullptr;
+  const bool with_ale = x->c.ale_zexist != 0;
+  const int G = 16;  // steps per graph launch
+  if (!x->gexec || x->gsteps != G || x->g_ale != with_ale || (!history) != (x->C.max_records == 0)) {
+    if (x->gexec) cudaGraphExecDestroy(x->gexec);
+    x->gexec = nullptr;
+    cudaGraph_t g;
+    r = cudaStreamBeginCapture(x->stream, cudaStreamCaptureModeThreadLocal);
+    if (r != cudaSuccess) return cuda_fail(e, r, "bl_run capture");
+    for (int k = 0; k < G; k++) {
+      x->L.getdt(x->F, x->C, x->stream);
+      x->L.lag_force(x->F, x->C, x->stream);
+      x->L.lag_accel(x->F, x->C, x->stream);
+      x->L.lag_state(x->F, x->C, x->stream);
+      if (with_ale) x->L.ale(x->F, x->C, x->stream);
+    }
+    r = cudaStreamEndCapture(x->stream, &g);
+    if (r != cudaSuccess) return cuda_fail(e, r, "bl_run capture");
+    r = cudaGraphInstantiate(&x->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (r != cudaSuccess) return cuda_fail(e, r, "bl_run instantiate");
+    x->gsteps = G;
+    x->g_ale = with_ale;
+  }
+  header_from_ts(x, ts, 1);
+  // step limit: getdt stops once nrecord reaches it (DevStep.nrecord counts)
+  int launched = 0;
+  const int per_step = bl::kLaunchesGetdt + bl::kLaunchesLagstep + (with_ale ? bl::kLaunchesAle : 0);
+  int done = 0;
+  while (true) {
+    const int remaining = max_steps - done;
+    if (remaining <= 0) break;
+    if (remaining >= G) {
+      r = cudaGraphLaunch(x->gexec, x->stream);
+      if (r != cudaSuccess) return cuda_fail(e, r, "bl_run launch");
+      x->launches += (long long)G * per_step;
+      launched += G;
+    } else {
+      for (int k = 0; k < remaining; k++) {
+        x->L.getdt(x->F, x->C, x->stream);
+        x->L.lag_force(x->F, x->C, x->stream);
+        x->L.lag_accel(x->F, x->C, x->stream);
+        x->L.lag_state(x->F, x->C, x->stream);
+        if (with_ale) x->L.ale(x->F, x->C, x->stream);
+      }
+      x->launches += (long long)remaining * per_step;
+      launched += remaining;
+    }
+    int rc = fetch_header(x, e, "bl_run");
+    if (rc != BL_SUCCESS) return rc;
+    done = x->hstep->nrecord;
+    if (x->hstep->halted || x->hstep->stop_next || x->hstep->err_code ||
+        x->hstep->negvol_pred || x->hstep->negvol_corr || x->hstep->negvol_ale)
+      break;
+    if (done >= max_steps) break;
+  }
+  const DevStep S = *x->hstep;
+  const int nrec = std::min(S.nrecord, max_steps);
+  if (nsteps) *nsteps = nrec;
+  if (history && nrec > 0) {
+    std::vector<bl::StepRec> tmp(nrec);
+    cudaMemcpy(tmp.data(), x->F.hist, sizeof(bl::StepRec) * nrec, cudaMemcpyDeviceToHost);
+    for (int i = 0; i < nrec; i++) {
+      history[i].time = tmp[i].time;
+      history[i].dt = tmp[i].dt;
+      history[i].nstep = tmp[i].nstep;
+      history[i].idtel = tmp[i].idtel;
+      history[i].sdt_code = tmp[i].sdt_code;
+      history[i].ierr = tmp[i].ierr;
+    }
+  }
+  x->F.hist = keep_hist;
+  x->cs2_is_v = false;
+  fill_ts_from_step(x, S, ts);
+  ts->zcorrector = 1;
+  ts->dts = ts->dt;
+  (void)launched;
+  if (S.err_code == 1) {
+    set_err(e, BL_FAILURE, BL_HALT_SINGLE, "ERROR: negative CFL condition in hydro_dr_getdt");
+    return BL_FAILURE;
+  }
+  if (S.err_code == 2) {
+    set_err(e, BL_FAILURE, BL_HALT_ALL, "ERROR: dt < dt_min");
+    return BL_FAILURE;
+  }
+  if (S.negvol_pred) return negvol_error(S.negvol_pred, e);
+  if (S.negvol_corr) return negvol_error(S.negvol_corr, e);
+  if (S.negvol_ale) return negvol_error(S.negvol_ale, e);
+  return BL_SUCCESS;
+}
+
+static size_t field_count(const bl_ctx* x, int id, int& kind) {
+  // kind: 0 double element, 1 double corner, 2 double node, 3 double comp,
+  //       4 derived (cnx/cny/cpa*), -1 not a device state field
+  const int nel = x->s.nel, nnd = x->s.nnd, ncp = x->s.ncp;
+  switch (id) {
+    case BL_ELDENSITY: case BL_ELENERGY: case BL_ELPRESSURE: case BL_ELCS2: case BL_ELVOLUME:
+    case BL_A1: case BL_A2: case BL_A3: case BL_B1: case BL_B2: case BL_B3: case BL_ELVISC:
+    case BL_ELMASS:
+      kind = 0;
+      return nel;
+    case BL_CNWT: case BL_CNVISCX: case BL_CNVISCY: case BL_CNMASS:
+      kind = 1;
+      return 4L * nel;
+    case BL_NDX: case BL_NDY: case BL_NDU: case BL_NDV:
+      kind = 2;
+      return nnd;
+    case BL_CPDENSITY: case BL_CPENERGY: case BL_CPPRESSURE: case BL_CPCS2: case BL_CPVOLUME:
+      kind = ncp > 0 ? 3 : -1;
+      return ncp;
+    case BL_CNX: case BL_CNY:
+      kind = 4;
+      return 4L * nel;
+    case BL_CPA1: case BL_CPA3: case BL_CPB1: case BL_CPB3:
+      kind = ncp > 0 ? 4 : -1;
+      return ncp;
+    default:
+      kind = -1;
+      return 0;
+  }
+}
+
+static void* dev_ptr(bl_ctx* x, int id) {
+  bl::DevFields& F = x->F;
+  switch (id) {
+    case BL_ELDENSITY: return F.rho;
+    case BL_ELENERGY: return F.e;
+    case BL_ELPRESSURE: return F.p;
+    case BL_ELCS2: return x->cs2_is_v ? F.cs2v : F.cs2;
+    case BL_ELVOLUME: return F.vol;
+    case BL_A1: return F.a1;
+    case BL_A2: return F.a2;
+    case BL_A3: return F.a3;
+    case BL_B1: return F.b1;
+    case BL_B2: return F.b2;
+    case BL_B3: return F.b3;
+    case BL_ELVISC: return F.visc;
+    case BL_ELMASS: return F.mass;
+    case BL_CNWT: return F.cnwt;
+    case BL_CNVISCX: return F.cnviscx;
+    case BL_CNVISCY: return F.cnviscy;
+    case BL_CNMASS: return F.cnmass;
+    case BL_NDX: return F.ndx;
+    case BL_NDY: return F.ndy;
+    case BL_NDU: return F.ndu;
+    case BL_NDV: return F.ndv;
+    case BL_CPDENSITY: return F.cprho;
+    case BL_CPENERGY: return F.cpe;
+    case BL_CPPRESSURE: return F.cpp;
+    case BL_CPCS2: return F.cpcs2;
+    case BL_CPVOLUME: return F.cpvol;
+    default: return nullptr;
+  }
+}
+
+int bl_sync_to_host(bl_ctx* x, int id) {
+  if (!x) return BL_FAILURE;
+  if (id == 0) {
+    for (int k : kStateIds) {
+      int rc = bl_sync_to_host(x, k);
+      if (rc != BL_SUCCESS) return rc;
+    }
+    return BL_SUCCESS;
+  }
+  if (id < 1 || id > BL_NID || !x->host[id]) return BL_SUCCESS;
+  int kind;
+  size_t n = field_count(x, id, kind);
+  if (kind < 0) return BL_SUCCESS;
+  cudaError_t r;
+  if (kind == 4) {
+    // derived fields: cnx/cny = node positions gathered to corners
+    // (utils_kn_cngather); cpa*/cpb* = element terms gathered to components
+    const int* ielnd = static_cast<const int*>(x->host[BL_IELND]);
+    double* h = static_cast<double*>(x->host[id]);
+    if (id == BL_CNX || id == BL_CNY) {
+      std::vector<double> nd(x->s.nnd);
+      r = cudaMemcpy(nd.data(), id == BL_CNX ? x->F.ndx : x->F.ndy, sizeof(double) * x->s.nnd,
+                     cudaMemcpyDeviceToHost);
+      if (r != cudaSuccess) return BL_FAILURE;
+      for (size_t k = 0; k < n; k++) h[k] = nd[ielnd[k] - 1];
+    } else {
+      const double* src = id == BL_CPA1 ? x->F.a1 : id == BL_CPA3 ? x->F.a3 : id == BL_CPB1 ? x->F.b1 : x->F.b3;
+      std::vector<double> el(x->s.nel);
+      r = cudaMemcpy(el.data(), src, sizeof(double) * x->s.nel, cudaMemcpyDeviceToHost);
+      if (r != cudaSuccess) return BL_FAILURE;
+      const int* imxel = static_cast<const int*>(x->host[BL_IMXEL]);
+      const int* imxfcp = static_cast<const int*>(x->host[BL_IMXFCP]);
+      const int* imxncp = static_cast<const int*>(x->host[BL_IMXNCP]);
+      for (int m = 0; m < x->s.nmx; m++)
+        for (int k = 0; k < imxncp[m]; k++) h[imxfcp[m] - 1 + k] = el[imxel[m] - 1];
+    }
+    return BL_SUCCESS;
+  }
+  r = cudaMemcpy(x->host[id], dev_ptr(x, id), n * sizeof(double), cudaMemcpyDeviceToHost);
+  return r == cudaSuccess ? BL_SUCCESS : BL_FAILURE;
+}
+
+int bl_sync_to_device(bl_ctx* x, int id) {
+  if (!x) return BL_FAILURE;
+  if (id == 0) {
+    for (int k : kStateIds) {
+      int rc = bl_sync_to_device(x, k);
+      if (rc != BL_SUCCESS) return rc;
+    }
+    return BL_SUCCESS;
+  }
+  if (id < 1 || id > BL_NID || !x->host[id]) return BL_SUCCESS;
+  int kind;
+  size_t n = field_count(x, id, kind);
+  if (kind < 0 || kind == 4) return BL_SUCCESS;
+  void* d = dev_ptr(x, id);
+  cudaError_t r = cudaMemcpy(d, x->host[id], n * sizeof(double), cudaMemcpyHostToDevice);
+  if (id == BL_ELCS2 && r == cudaSuccess)  // keep both copies of elcs2 equal
+    r = cudaMemcpy(x->cs2_is_v ? x->F.cs2 : x->F.cs2v, x->host[id], n * sizeof(double),
+                   cudaMemcpyHostToDevice);
+  return r == cudaSuccess ? BL_SUCCESS : BL_FAILURE;
+}
+
+int bl_synchronize(bl_ctx* x) {
+  if (!x) return BL_FAILURE;
+  return (int)cudaStreamSynchronize(x->stream);
+}
+
+void* bl_stream(bl_ctx* x) { return x ? (void*)x->stream : nullptr; }
+
+long long bl_kernel_launches(bl_ctx* x) { return x ? x->launches : 0; }
+
+// Struct sizes, so a host binding can check its mirrors of the header.
+int bl_abi_sizes(int* out, int n) {
+  const int v[5] = {(int)sizeof(bl_sizes), (int)sizeof(bl_config), (int)sizeof(bl_timestep),
+                    (int)sizeof(bl_error), (int)sizeof(bl_step_record)};
+  for (int i = 0; i < n && i < 5; i++) out[i] = v[i];
+  return 5;
+}
+
+}  // extern "C"

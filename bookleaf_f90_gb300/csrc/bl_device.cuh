@@ -1,0 +1,130 @@
+// bl_device.cuh -- device-side data structures and helpers shared by the
+// hydro (Lagrangian) and ALE kernels.
+//
+// Layout in HBM (one partition, structure of arrays):
+//   node fields     double[nnd]            ndx, ndy, ndu, ndv, ndubar, ...
+//   element fields  double[nel]            eldensity, elenergy, ...
+//   corner fields   d4[nel]           cnwt, cnmass, cnviscx, ... (the
+//                                          reference's (NCORN,nel) block: the
+//                                          4 corners of one element are one
+//                                          32-byte vector load)
+//   connectivity    int4[nel] (0-based)    ielnd, ielel; ielfc packed as four
+//                                          bytes in one int
+//   node->corner    CSR (offsets, entries) in the summation order of the
+//                   reference's scatter loops, so node sums are computed by
+//                   gathers without atomics and are deterministic.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace bl {
+
+// 32-byte aligned vector of the four corner (or face) values of one element.
+using d4 = double4_32a;
+__host__ __device__ __forceinline__ d4 make_d4(double x, double y, double z, double w) {
+  return make_double4_32a(x, y, z, w);
+}
+
+// Runtime state of the time loop that lives on the device.  The host reads
+// it back once per bl_getdt call; bl_run never reads it inside the loop.
+struct DevStep {
+  double time, dt, dts;
+  double cfl_rdt, div_rdt;
+  int nstep, idtel, sdt, imdt;
+  int cfl_idt, div_idt;
+  int ierr, iout;       // error_t of the first failure
+  int err_code;         // 0 none, 1 negative CFL, 2 dt<dt_min, 3 neg volume
+  int negvol_pred;      // 1 + last element with V<0 in the predictor (0: none)
+  int negvol_corr;      // same for the corrector
+  int negvol_ale;       // same for the ALE update
+  int run_mode;         // 1 inside bl_run: kernels stop after time_end/error
+  int stop_next;        // set by getdt when time >= time_end (bl_run)
+  int halted;           // kernels return at once when set
+  int nrecord;          // steps recorded in the history buffer
+  unsigned int ticket;  // last-block counter of the dt reduction
+  int pad;
+};
+
+struct StepRec {        // mirrors bl_step_record
+  double time, dt;
+  int nstep, idtel, sdt_code, ierr;
+};
+
+// Configuration scalars and the small per-region / per-material tables.
+struct DevCfg {
+  double cvisc1, cvisc2, cfl_sf, div_sf;
+  double zcut, zerocut, dencut, accut, ccut, pcut;
+  double dt_g, dt_min, dt_max, dt_initial, time_end;
+  double ale_mintime, ale_maxtime;
+  int ztq, zhg, zsp, nreg, nmat, ale_zexist, ale_zeul, adv_type;
+  int max_records, pad0;
+  const double* kappareg;    // [nreg]
+  const double* pmeritreg;   // [nreg]
+  const int* zdtnotreg;      // [nreg]
+  const int* zmidlength;     // [nreg]
+  const int* eos_type;       // [nmat+1]
+  const double* eos_param;   // [(nmat+1)*6]
+  const double* eos_gm1;     // [nmat+1]  param1-1           (ideal gas)
+  const double* eos_ggm1;    // [nmat+1]  param1*(param1-1)  (ideal gas)
+};
+
+struct DevFields {
+  int nel, nnd, ncp, nmx;
+  // connectivity (0-based)
+  const int4* ielnd;
+  const int4* ielel;
+  const int* ielfc;          // 4 x 8-bit face numbers 0..3
+  const int* ielreg;         // 0-based region
+  const int* ielmat;         // material (<=0: mixed / void)
+  const int* indtype;
+  const int* elmx;           // mixed-cell index of an element (-1: pure)
+  // node -> corner CSR, corner-major order (hydro_kn_scatteracceleration)
+  const int* nc_off;         // [nnd+1]
+  const int* nc_ent;         // entries 4*iel+corner
+  // node -> corner CSR, element-major order (ALE nodal sums)
+  const int* ne_off;
+  const int* ne_ent;
+  // node fields
+  double *ndx, *ndy, *ndu, *ndv, *ndubar, *ndvbar, *ndxn, *ndyn;
+  // element fields
+  double *rho, *e, *p, *cs2, *cs2v, *vol, *mass, *visc;
+  double *a1, *a2, *a3, *b1, *b2, *b3;
+  double *rho_h;             // half-step density (predictor -> node kernel)
+  double* e_scr;             // elenergy0 / ALE scratch
+  // corner fields
+  d4 *cnwt, *cnmass, *cnviscx, *cnviscy, *cnfx, *cnfy, *spmass;
+  d4* cnwt_h;           // half-step corner volumes
+  // mixed cells (flattened; components of one cell contiguous)
+  const int* imxel;          // 0-based element of a mixed cell
+  const int* imxfcp;         // 0-based first component
+  const int* imxncp;
+  const int* icpmat;
+  double *cprho, *cpe, *cpp, *cpcs2, *cpvol, *frvol, *cpm, *frm, *cpvisc;
+  d4 *cpviscx, *cpviscy, *cpfx, *cpfy;
+  // ALE scratch
+  d4 *fcdv, *fcdm, *eflux, *cndm, *cnflux, *cnfu, *cnfv, *cnm0, *cnmass_new;
+  double *vpr, *mpr, *cutm_el;
+  double* rscr25;            // split-advection stale-scratch emulation (unused)
+  // dt reduction partials
+  double* red_v;             // [2*nblk]
+  int* red_i;                // [2*nblk]
+  DevStep* step;
+  StepRec* hist;
+};
+
+// ---------------------------------------------------------------- helpers
+
+// Fortran MAX/MIN as the CPU restatement evaluates them: the first argument
+// is returned on ties.
+__device__ __forceinline__ double maxF(double a, double b) { return (b > a) ? b : a; }
+__device__ __forceinline__ double minF(double a, double b) { return (b < a) ? b : a; }
+// Fortran SIGN(a,b): |a| with the sign bit of b (negative zero honoured).
+__device__ __forceinline__ double signF(double a, double b) { return copysign(fabs(a), b); }
+
+__device__ __forceinline__ int fc_of(int packed, int j) { return (packed >> (8 * j)) & 0xff; }
+
+__device__ __forceinline__ double c4(const d4& v, int j) {
+  return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
+}
+
+}  // namespace bl

@@ -1,0 +1,41 @@
+// bl_kernels.h -- launch functions of the kernel translation unit.
+//
+// bl_kernels.cu is compiled twice: once as namespace bl::exact with
+// --fmad=false (bit-reproducible against a -ffp-contract=off CPU build) and
+// once as namespace bl::fast with --fmad=true.  The C-ABI layer picks one
+// table per context (bl_init's fp_mode).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "bl_device.cuh"
+
+namespace bl {
+
+#define BL_DECLARE_LAUNCHERS(NS)                                                   \
+  namespace NS {                                                                   \
+  int getdt_blocks(int nel);                                                       \
+  void launch_getdt(const DevFields& F, const DevCfg& C, cudaStream_t s);          \
+  void launch_lag_force(const DevFields& F, const DevCfg& C, cudaStream_t s);      \
+  void launch_lag_accel(const DevFields& F, const DevCfg& C, cudaStream_t s);      \
+  void launch_lag_state(const DevFields& F, const DevCfg& C, cudaStream_t s);      \
+  void launch_ale(const DevFields& F, const DevCfg& C, cudaStream_t s);            \
+  }
+
+BL_DECLARE_LAUNCHERS(fast)
+BL_DECLARE_LAUNCHERS(exact)
+
+struct Launchers {
+  int (*getdt_blocks)(int);
+  void (*getdt)(const DevFields&, const DevCfg&, cudaStream_t);
+  void (*lag_force)(const DevFields&, const DevCfg&, cudaStream_t);
+  void (*lag_accel)(const DevFields&, const DevCfg&, cudaStream_t);
+  void (*lag_state)(const DevFields&, const DevCfg&, cudaStream_t);
+  void (*ale)(const DevFields&, const DevCfg&, cudaStream_t);
+};
+
+// Kernels launched by one call of each launcher (for bl_kernel_launches).
+constexpr int kLaunchesGetdt = 1;
+constexpr int kLaunchesLagstep = 3;
+constexpr int kLaunchesAle = 4;
+
+}  // namespace bl

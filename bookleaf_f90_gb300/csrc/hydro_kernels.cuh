@@ -1,0 +1,865 @@
+// hydro_kernels.cu -- the Lagrangian hot path on sm_103a.
+//
+// Four kernels per step replace the reference's sequence of loops:
+//   k_getdt        inf_solver_getdt: utils_kn_cngather u,v; the three edge-
+//                  viscosity loops (hydro_kn_edgeviscosity.f90:30-282);
+//                  hydro_dr_getcs2; hydro_kn_getdtcfl / getdtdiv
+//                  (hydro_kn_getdt.f90:30-122) with the two argmin/argmax
+//                  scans done as a block reduction plus a last-block pass
+//                  that also runs time_dr_end (time_dr_advance.f90:74-132).
+//   k_lag_force    inf_solver_lagstep up to the corrector force: predictor
+//                  force (hydro_kn_getforce.f90), half-step vertices,
+//                  geometry, density, energy, EoS, then the corrector force
+//                  with hourglass and sub-zonal terms, and the mixed-cell
+//                  force average (hydro_dr_getacceleration.f90:61-79).
+//   k_lag_accel    hydro_kn_scatteracceleration/getacceleration/
+//                  applyacceleration and utils_kn_bc per node, gathering
+//                  corner contributions over a CSR in the reference's loop
+//                  order; writes u^{n+1}, ubar and the final vertices.
+//   k_lag_state    the corrector getstate: geometry at x^{n+1}, density,
+//                  energy from e^n with the corrector forces and ubar, EoS.
+//
+// Every expression keeps the reference's operand order.  This file is
+// compiled twice: with --fmad=false (namespace exact) the results equal the
+// CPU restatement bit for bit; with --fmad=true (namespace fast) the compiler
+// may fuse multiply-adds.
+#pragma once
+#include <cfloat>
+#include <cmath>
+
+#include "bl_device.cuh"
+#include "bl_kernels.h"
+
+namespace bl {
+namespace BL_NS {
+
+// ------------------------------------------------------------------ EoS
+// eos_kn_getpressure / eos_kn_getcs2 (eos_kn_forms.f90:28-106)
+__device__ __forceinline__ void eos_pc(const DevCfg& C, int mat, double rho, double e,
+                                       double& p, double& cs2) {
+  const int imat = mat > 0 ? mat : 0;
+  const int t = __ldg(C.eos_type + imat);
+  const double* P = C.eos_param + 6 * imat;
+  if (t == 1) {
+    p = e * rho * __ldg(C.eos_gm1 + imat);
+    cs2 = __ldg(C.eos_ggm1 + imat) * e;
+  } else if (t == 0) {
+    p = __ldg(P);
+    cs2 = C.ccut;
+  } else if (t == 2) {
+    double t1 = rho / __ldg(P + 2);
+    p = __ldg(P) * (pow(t1, __ldg(P + 1)) - 1.0);
+    p = maxF(p, __ldg(P + 3));
+    double t2 = __ldg(P + 1) - 1.0;
+    cs2 = (__ldg(P) * __ldg(P + 1)) / __ldg(P + 2);
+    cs2 = cs2 * pow(t1, t2);
+  } else if (t == 3) {
+    double t1 = __ldg(P + 3) * __ldg(P + 5) / rho;
+    double t2 = __ldg(P + 4) * __ldg(P + 5) / rho;
+    double t3 = __ldg(P) * rho * e;
+    double t4 = (1.0 - __ldg(P) / t1) * __ldg(P + 1) * exp(-t1);
+    double t5 = (1.0 - __ldg(P) / t2) * __ldg(P + 2) * exp(-t2);
+    p = t3 + t4 + t5;
+    double pp = p;
+    if (fabs(pp) < C.pcut) pp = 0.0;
+    double q1 = __ldg(P + 5) / rho;
+    double s3 = __ldg(P + 3) * q1;
+    double u4 = __ldg(P) / __ldg(P + 3) + __ldg(P) * q1 - s3 * q1;
+    u4 = u4 * __ldg(P + 1) * exp(-s3);
+    s3 = __ldg(P + 4) * q1;
+    double u5 = __ldg(P) / __ldg(P + 4) + __ldg(P) * q1 - s3 * q1;
+    u5 = u5 * __ldg(P + 2) * exp(-s3);
+    cs2 = __ldg(P) * pp / rho + __ldg(P) * e - u4 - u5;
+  } else {
+    p = -1.0;
+    cs2 = C.ccut;
+  }
+  if (fabs(p) < C.pcut) p = 0.0;
+  cs2 = maxF(cs2, C.ccut);
+}
+
+// ------------------------------------------------------------------ geometry
+// geometry_kn_getiso + getvolume (geometry_kn_volume.f90:30-79)
+struct Iso {
+  double a1, a2, a3, b1, b2, b3, w0, w1, w2, w3, vol;
+};
+
+__device__ __forceinline__ Iso getiso(const double* x, const double* y) {
+  Iso g;
+  g.a1 = 0.25 * (-x[0] + x[1] + x[2] - x[3]);
+  g.a2 = 0.25 * (x[0] - x[1] + x[2] - x[3]);
+  g.a3 = 0.25 * (-x[0] - x[1] + x[2] + x[3]);
+  g.b1 = 0.25 * (-y[0] + y[1] + y[2] - y[3]);
+  g.b2 = 0.25 * (y[0] - y[1] + y[2] - y[3]);
+  g.b3 = 0.25 * (-y[0] - y[1] + y[2] + y[3]);
+  const double o9 = 1.0 / 9.0;
+  const double A1m = 3.0 * g.a1 - g.a2, A1p = 3.0 * g.a1 + g.a2;
+  const double A3m = 3.0 * g.a3 - g.a2, A3p = 3.0 * g.a3 + g.a2;
+  const double B1m = 3.0 * g.b1 - g.b2, B1p = 3.0 * g.b1 + g.b2;
+  const double B3m = 3.0 * g.b3 - g.b2, B3p = 3.0 * g.b3 + g.b2;
+  g.w0 = o9 * (B3m * A1m - A3m * B1m);
+  g.w1 = o9 * (B3p * A1m - A3p * B1m);
+  g.w2 = o9 * (B3p * A1p - A3p * B1p);
+  g.w3 = o9 * (B3m * A1p - A3m * B1p);
+  g.vol = 4.0 * (g.a1 * g.b3 - g.a3 * g.b1);
+  return g;
+}
+
+// geometry_kn_length (geometry_kn_length.f90:99-139)
+__device__ __forceinline__ double g_denom(double x1, double y1, double x2, double y2) {
+  double w1 = y1 - y2, w2 = x1 - x2;
+  return w1 * w1 + w2 * w2;
+}
+__device__ __forceinline__ double g_distpp(double x3, double y3, double x4, double y4, double x1,
+                                           double y1) {
+  double w1 = 0.5 * (x3 + x4) - x1;
+  double w2 = 0.5 * (y3 + y4) - y1;
+  return w1 * w1 + w2 * w2;
+}
+__device__ __forceinline__ double g_distpl(double x3, double y3, double x4, double y4, double x1,
+                                           double y1, double x2, double y2) {
+  double res = 0.5 * (y1 - y2) * (x3 + x4) + 0.5 * (y3 + y4) * (x2 - x1) + y2 * x1 - y1 * x2;
+  return res * res;
+}
+
+// MINVAL(geometry_kn_dln(...)) (geometry_kn_length.f90:58-97)
+__device__ __forceinline__ double min_dln(const double* x, const double* y, double zcut) {
+  double r[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    // res(k+1): denominator from corners k+2,k+3; distance of corners
+    // k,k+1 midpoint... in the reference's argument order
+    const int a = k, b = (k + 1) & 3, c = (k + 2) & 3, d = (k + 3) & 3;
+    double w1 = g_denom(x[c], y[c], x[d], y[d]);
+    if (w1 < zcut) r[k] = g_distpp(x[a], y[a], x[b], y[b], x[c], y[c]);
+    else r[k] = g_distpl(x[a], y[a], x[b], y[b], x[c], y[c], x[d], y[d]) / w1;
+  }
+  double m = r[0];
+  m = minF(m, r[1]);
+  m = minF(m, r[2]);
+  m = minF(m, r[3]);
+  return m;
+}
+
+// MINVAL(geometry_kn_dlm(...)) (geometry_kn_length.f90:30-56)
+__device__ __forceinline__ double min_dlm(const double* x, const double* y) {
+  double x1 = x[0] + x[1], x2 = x[2] + x[3], y1 = y[0] + y[1], y2 = y[2] + y[3];
+  x1 = 0.5 * (x1 - x2);
+  y1 = 0.5 * (y1 - y2);
+  double r0 = x1 * x1 + y1 * y1;
+  x1 = x[2] + x[1];
+  x2 = x[0] + x[3];
+  y1 = y[2] + y[1];
+  y2 = y[0] + y[3];
+  x1 = 0.5 * (x1 - x2);
+  y1 = 0.5 * (y1 - y2);
+  double r1 = x1 * x1 + y1 * y1;
+  double m = r0;
+  m = minF(m, r1);
+  m = minF(m, r0);
+  m = minF(m, r1);
+  return m;
+}
+
+// ------------------------------------------------------------------ forces
+// hydro_kn_getforceP + getforceQ (hydro_kn_getforce.f90:30-71)
+__device__ __forceinline__ void force_pq(double p, double a1, double a3, double b1, double b3,
+                                         const d4& qx, const d4& qy, double* fx,
+                                         double* fy) {
+  fx[0] = p * (-b3 + b1);
+  fx[1] = p * (b3 + b1);
+  fx[2] = p * (b3 - b1);
+  fx[3] = p * (-b3 - b1);
+  fy[0] = p * (a3 - a1);
+  fy[1] = p * (-a3 - a1);
+  fy[2] = p * (-a3 + a1);
+  fy[3] = p * (a3 + a1);
+  fx[0] = fx[0] + qx.x;
+  fy[0] = fy[0] + qy.x;
+  fx[1] = fx[1] + qx.y;
+  fy[1] = fy[1] + qy.y;
+  fx[2] = fx[2] + qx.z;
+  fy[2] = fy[2] + qy.z;
+  fx[3] = fx[3] + qx.w;
+  fy[3] = fy[3] + qy.w;
+}
+
+// hydro_kn_getforceSP (hydro_kn_getforce.f90:109-188)
+__device__ void force_sp(double w1, double rho, double cs2, const double* cx, const double* cy,
+                         const d4& spm, double* fx, double* fy) {
+  double x3 = 0.25 * (cx[0] + cx[1] + cx[2] + cx[3]);
+  double y3 = 0.25 * (cy[0] + cy[1] + cy[2] + cy[3]);
+  double lfx[4][4], lfy[4][4];
+#pragma unroll
+  for (int j1 = 0; j1 < 4; j1++) {
+    double x1 = cx[j1], y1 = cy[j1];
+    int j2 = (j1 + 1) & 3;
+    double x2 = 0.5 * (x1 + cx[j2]), y2 = 0.5 * (y1 + cy[j2]);
+    j2 = (j1 + 3) & 3;
+    double x4 = 0.5 * (x1 + cx[j2]), y4 = 0.5 * (y1 + cy[j2]);
+    double w3 = 0.25 * (-x1 + x2 + x3 - x4);
+    double w4 = 0.25 * (-x1 - x2 + x3 + x4);
+    double w5 = 0.25 * (-y1 + y2 + y3 - y4);
+    double w6 = 0.25 * (-y1 - y2 + y3 + y4);
+    double w2 = 4.0 * (w3 * w6 - w4 * w5);
+    w2 = c4(spm, j1) / w2;
+    w2 = w2 - rho;
+    w2 = cs2 * w2;
+    lfx[j1][0] = w2 * (w5 - w6);
+    lfx[j1][1] = w2 * (w5 + w6);
+    lfx[j1][2] = w2 * (-w5 + w6);
+    lfx[j1][3] = w2 * (-w5 - w6);
+    lfy[j1][0] = w2 * (-w3 + w4);
+    lfy[j1][1] = w2 * (-w3 - w4);
+    lfy[j1][2] = w2 * (w3 - w4);
+    lfy[j1][3] = w2 * (w3 + w4);
+  }
+  double w2 = 0.5 * (lfx[0][3] + lfx[3][1]);
+  double w3 = 0.5 * (lfx[0][1] + lfx[1][3]);
+  double w4 = 0.5 * (lfx[1][1] + lfx[2][3]);
+  double w5 = 0.5 * (lfx[3][3] + lfx[2][1]);
+  double w6 = 0.25 * (lfx[0][2] + lfx[1][2] + lfx[2][2] + lfx[3][2]);
+  fx[0] = fx[0] + w1 * (lfx[0][0] + w2 + w3 + w6);
+  fx[1] = fx[1] + w1 * (lfx[1][0] + w4 + w3 + w6);
+  fx[2] = fx[2] + w1 * (lfx[2][0] + w4 + w5 + w6);
+  fx[3] = fx[3] + w1 * (lfx[3][0] + w2 + w5 + w6);
+  w2 = 0.5 * (lfy[0][3] + lfy[3][1]);
+  w3 = 0.5 * (lfy[0][1] + lfy[1][3]);
+  w4 = 0.5 * (lfy[1][1] + lfy[2][3]);
+  w5 = 0.5 * (lfy[3][3] + lfy[2][1]);
+  w6 = 0.25 * (lfy[0][2] + lfy[1][2] + lfy[2][2] + lfy[3][2]);
+  fy[0] = fy[0] + w1 * (lfy[0][0] + w2 + w3 + w6);
+  fy[1] = fy[1] + w1 * (lfy[1][0] + w4 + w3 + w6);
+  fy[2] = fy[2] + w1 * (lfy[2][0] + w4 + w5 + w6);
+  fy[3] = fy[3] + w1 * (lfy[3][0] + w2 + w5 + w6);
+}
+
+// hydro_kn_getforceHG (hydro_kn_getforce.f90:73-107)
+__device__ __forceinline__ void force_hg(double kappa, double rho, double area, double rdt,
+                                         const double* u, const double* v, double* fx,
+                                         double* fy) {
+  double w2 = u[0] - u[1] + u[2] - u[3];
+  double w3 = v[0] - v[1] + v[2] - v[3];
+  double w1 = -kappa * rho * area * rdt;
+  w2 = w1 * w2;
+  w3 = w1 * w3;
+  fx[0] = fx[0] + w2;
+  fx[1] = fx[1] - w2;
+  fx[2] = fx[2] + w2;
+  fx[3] = fx[3] - w2;
+  fy[0] = fy[0] + w3;
+  fy[1] = fy[1] - w3;
+  fy[2] = fy[2] + w3;
+  fy[3] = fy[3] - w3;
+}
+
+// hydro_kn_getenergy (hydro_kn_getenergy.f90:29-52): the increment w1*dt
+__device__ __forceinline__ double energy_update(double e, double m, double zerocut, double dt,
+                                                const double* fx, const double* fy,
+                                                const double* u, const double* v) {
+  double w1 = fx[0] * u[0] + fy[0] * v[0] + fx[1] * u[1] + fy[1] * v[1] + fx[2] * u[2] +
+              fy[2] * v[2] + fx[3] * u[3] + fy[3] * v[3];
+  w1 = -(w1 / maxF(m, zerocut));
+  return e + w1 * dt;
+}
+
+__device__ __forceinline__ bool halted(const DevStep* S) {
+  return *((volatile const int*)&S->halted) != 0;
+}
+
+// ================================================================ k_getdt
+
+// (value,index) pairs for the two scans.  CFL: smallest value, first index
+// on ties (hydro_kn_getdt.f90:70-73).  DIV: largest value above TINY, first
+// index on ties, (TINY,-1) when no element exceeds TINY (:103-116).
+__device__ __forceinline__ void cfl_min(double& v, int& i, double ov, int oi) {
+  if (ov < v || (ov == v && oi < i)) { v = ov; i = oi; }
+}
+__device__ __forceinline__ void div_max(double& v, int& i, double ov, int oi) {
+  if (ov > v || (ov == v && oi >= 0 && (i < 0 || oi < i))) { v = ov; i = oi; }
+}
+
+template <int BS>
+__global__ void __launch_bounds__(BS) k_getdt(DevFields F, DevCfg C) {
+  DevStep* S = F.step;
+  if (halted(S)) return;
+  if (S->stop_next) {            // bl_run: the previous step reached time_end
+    if (blockIdx.x == 0 && threadIdx.x == 0) S->halted = 1;
+    return;
+  }
+  const int iel = blockIdx.x * BS + threadIdx.x;
+  double cflv = HUGE_VAL;        // sentinel above HUGE(1.0)
+  int cfli = 0x7fffffff;
+  double divv = DBL_MIN;         // TINY(1.0)
+  int divi = -1;
+  if (iel < F.nel) {
+    const int4 nd = __ldg(F.ielnd + iel);
+    const int n[4] = {nd.x, nd.y, nd.z, nd.w};
+    double x[4], y[4], u[4], v[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      x[j] = F.ndx[n[j]];
+      y[j] = F.ndy[n[j]];
+      u[j] = F.ndu[n[j]];
+      v[j] = F.ndv[n[j]];
+    }
+    const double zc = C.zerocut;
+    const double rho0 = F.rho[iel];
+    double visc = 0.0;
+    double qx[4] = {0.0, 0.0, 0.0, 0.0}, qy[4] = {0.0, 0.0, 0.0, 0.0};
+    if (!C.ztq) {
+      // hydro_kn_initeviscosity: face j runs corner j -> j+1
+      double du[4], dv[4], dx[4], dy[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const int jn = (j + 1) & 3;
+        du[j] = u[jn] - u[j];
+        dv[j] = v[jn] - v[j];
+        dx[j] = x[jn] - x[j];
+        dy[j] = y[jn] - y[j];
+      }
+      const int4 ee = __ldg(F.ielel + iel);
+      const int nb[4] = {ee.x, ee.y, ee.z, ee.w};
+      const int fcp = __ldg(F.ielfc + iel);
+      // per own face: |du|, 1/max(|du|,zc)-normalised (uhat,vhat), |dx|,
+      // (xhat,yhat) and the inverse of the own normalised gradient w1
+      double lu[4], lx[4], uh[4], vh[4], xh[4], yh[4];
+      double sc[4][2];  // limiter ratios (neighbour across s, across s+2)
+      double edv[4];
+#pragma unroll
+      for (int s = 0; s < 2; s++) {
+        const int in1 = nb[s], in2 = nb[s + 2];
+        const int f1 = fc_of(fcp, s), f2 = fc_of(fcp, s + 2);
+#pragma unroll
+        for (int e2 = 0; e2 < 2; e2++) {
+          const int is = e2 == 0 ? ((s + 3) & 3) : (s + 1);
+          double w1 = du[is], w2 = dv[is], w3 = dx[is], w4 = dy[is];
+          double den = sqrt(w1 * w1 + w2 * w2);
+          lu[is] = den;
+          den = 1.0 / maxF(den, zc);
+          double uhat = w1 * den, vhat = w2 * den;
+          den = sqrt(w3 * w3 + w4 * w4);
+          lx[is] = den;
+          den = 1.0 / maxF(den, zc);
+          double xhat = w3 * den, yhat = w4 * den;
+          uh[is] = uhat;
+          vh[is] = vhat;
+          xh[is] = xhat;
+          yh[is] = yhat;
+          den = w3 * xhat + w4 * yhat;
+          w1 = (w1 * uhat + w2 * vhat) / signF(maxF(fabs(den), zc), den);
+          w1 = 1.0 / signF(maxF(fabs(w1), zc), w1);
+          // neighbour faces: edge 1 uses MOD(ielfc,4)+1 / MOD(ielfc+2,4)+1,
+          // edge 2 the other pair (hydro_kn_edgeviscosity.f90:117-151)
+          const int ins1 = e2 == 0 ? ((f1 + 1) & 3) : ((f1 + 3) & 3);
+          const int ins2 = e2 == 0 ? ((f2 + 3) & 3) : ((f2 + 1) & 3);
+          double r1 = 0.0, r2 = 0.0;
+          if (in1 != iel) {  // overwritten by the boundary rule otherwise
+            const int4 m = __ldg(F.ielnd + in1);
+            const int mm[4] = {m.x, m.y, m.z, m.w};
+            const int a = mm[ins1], b = mm[(ins1 + 1) & 3];
+            double ddx = F.ndx[b] - F.ndx[a], ddy = F.ndy[b] - F.ndy[a];
+            double ddu = F.ndu[b] - F.ndu[a], ddv = F.ndv[b] - F.ndv[a];
+            double dn = ddx * xhat + ddy * yhat;
+            double q = (ddu * uhat + ddv * vhat) / signF(maxF(fabs(dn), zc), dn);
+            r1 = q * w1;
+          }
+          if (in2 != iel) {
+            const int4 m = __ldg(F.ielnd + in2);
+            const int mm[4] = {m.x, m.y, m.z, m.w};
+            const int a = mm[ins2], b = mm[(ins2 + 1) & 3];
+            double ddx = F.ndx[b] - F.ndx[a], ddy = F.ndy[b] - F.ndy[a];
+            double ddu = F.ndu[b] - F.ndu[a], ddv = F.ndv[b] - F.ndv[a];
+            double dn = ddx * xhat + ddy * yhat;
+            double q = (ddu * uhat + ddv * vhat) / signF(maxF(fabs(dn), zc), dn);
+            r2 = q * w1;
+          }
+          sc[is][0] = r1;
+          sc[is][1] = r2;
+        }
+        // boundary rule (hydro_kn_edgeviscosity.f90:154-183)
+        const int is1 = (s + 3) & 3, is2 = s + 1;
+        if (in1 == iel) {
+          const int ic1 = n[s], ic2 = n[(s + 1) & 3];
+          const double val = (__ldg(F.indtype + ic1) < 0 && __ldg(F.indtype + ic2) < 0 && in2 != iel) ? 1.0 : 0.0;
+          sc[is1][0] = val;
+          sc[is2][0] = val;
+        }
+        if (in2 == iel) {
+          const int ic1 = n[s + 2], ic2 = n[(s + 3) & 3];
+          const double val = (__ldg(F.indtype + ic1) < 0 && __ldg(F.indtype + ic2) < 0 && in1 != iel) ? 1.0 : 0.0;
+          sc[is1][1] = val;
+          sc[is2][1] = val;
+        }
+        // apply limiter (hydro_kn_edgeviscosity.f90:185-214)
+        const double cs2i = F.cs2[iel];
+#pragma unroll
+        for (int e2 = 0; e2 < 2; e2++) {
+          const int is = e2 == 0 ? is1 : is2;
+          const int ins = nb[is];
+          double w1 = C.cvisc1 * sqrt(0.5 * (cs2i + F.cs2[ins]));
+          double w2 = sc[is][0], w3 = sc[is][1];
+          w2 = minF(minF(minF(0.5 * (w2 + w3), 2.0 * w2), 2.0 * w3), 1.0);
+          w2 = maxF(0.0, w2);
+          double w4 = lu[is];
+          w3 = 0.5 * (1.0 - w2) * (rho0 + F.rho[ins]) * (w1 + C.cvisc2 * w4);
+          edv[is] = w3;
+          w4 = 2.0 * w4 / maxF(rho0, zc);
+          visc = maxF(visc, w3 * w4);
+        }
+      }
+      // hydro_kn_geteviscosity (hydro_kn_edgeviscosity.f90:219-282)
+      const double xc = 0.25 * (x[0] + x[1] + x[2] + x[3]);
+      const double yc = 0.25 * (y[0] + y[1] + y[2] + y[3]);
+      double edx[4], edy[4];
+#pragma unroll
+      for (int f = 0; f < 4; f++) {
+        const int ins = (f + 1) & 3;
+        double w3 = 0.5 * (x[f] + x[ins]);
+        double w6 = 0.5 * (y[f] + y[ins]);
+        double w7 = sqrt((xc - w3) * (xc - w3) + (yc - w6) * (yc - w6));
+        double w8 = lx[f];  // SQRT(w1*w1+w4*w4) of the same face difference
+        double den = 1.0 / w7;
+        double xhat = (yc - w6) * den, yhat = (w3 - xc) * den;
+        // w1*(1/w8), w4*(1/w8): equal to the limiter's normalised face
+        // vector whenever w8 > zerocut; otherwise the edge is cut below
+        double q1 = xh[f], q2 = yh[f];
+        double w33 = xhat * q1 + yhat * q2;
+        den = -(signF(1.0, w33) * w7);
+        xhat = xhat * den;
+        yhat = yhat * den;
+        double uhat = du[f], vhat = dv[f];
+        double w5 = lu[f];
+        double w6b = uhat * xhat + vhat * yhat;
+        den = w6b / maxF(w5, zc);
+        edx[f] = edv[f] * uhat * den;
+        edy[f] = edv[f] * vhat * den;
+        if ((w5 <= zc) || (w6b <= zc) || (w7 <= zc) || (w8 <= zc)) {
+          edx[f] = 0.0;
+          edy[f] = 0.0;
+        }
+      }
+      qx[0] = edx[0] - edx[3];
+      qx[1] = edx[1] - edx[0];
+      qx[2] = edx[2] - edx[1];
+      qx[3] = edx[3] - edx[2];
+      qy[0] = edy[0] - edy[3];
+      qy[1] = edy[1] - edy[0];
+      qy[2] = edy[2] - edy[1];
+      qy[3] = edy[3] - edy[2];
+      F.cnviscx[iel] = make_d4(qx[0], qx[1], qx[2], qx[3]);
+      F.cnviscy[iel] = make_d4(qy[0], qy[1], qy[2], qy[3]);
+      F.visc[iel] = visc;
+    } else {
+      visc = F.visc[iel];
+    }
+    // hydro_dr_getcs2: elcs2 += elvisc; mixed cells: sum frmass*(cpcs2+cpvisc)
+    double cs2v = F.cs2[iel] + visc;
+    const int imx = F.elmx ? F.elmx[iel] : -1;
+    if (imx >= 0) {
+      double w1 = 0.0;
+      const int c0 = F.imxfcp[imx], nc = F.imxncp[imx];
+      for (int k = 0; k < nc; k++) w1 = w1 + F.frm[c0 + k] * (F.cpcs2[c0 + k] + F.cpvisc[c0 + k]);
+      cs2v = w1;
+    }
+    F.cs2v[iel] = cs2v;
+    // hydro_kn_getdtcfl
+    const int ireg = __ldg(F.ielreg + iel);
+    double r11;
+    if (__ldg(C.zdtnotreg + ireg)) {
+      r11 = DBL_MAX;
+    } else {
+      double w1 = __ldg(C.zmidlength + ireg) ? min_dlm(x, y) : min_dln(x, y, C.zcut);
+      r11 = w1 / cs2v;
+    }
+    cflv = r11;
+    cfli = iel;
+    // hydro_kn_getdtdiv
+    const double A1 = F.a1[iel], A3 = F.a3[iel], B1 = F.b1[iel], B3 = F.b3[iel];
+    double w1 = u[0] * (-B3 + B1) + v[0] * (A3 - A1) + u[1] * (B3 + B1) + v[1] * (-A3 - A1) +
+                u[2] * (B3 - B1) + v[2] * (-A3 + A1) + u[3] * (-B3 - B1) + v[3] * (A3 + A1);
+    w1 = fabs(w1) / F.vol[iel];
+    if (w1 > divv) {
+      divv = w1;
+      divi = iel;
+    }
+  }
+  // ---- block reduction
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    double ov = __shfl_xor_sync(0xffffffffu, cflv, o);
+    int oi = __shfl_xor_sync(0xffffffffu, cfli, o);
+    cfl_min(cflv, cfli, ov, oi);
+    ov = __shfl_xor_sync(0xffffffffu, divv, o);
+    oi = __shfl_xor_sync(0xffffffffu, divi, o);
+    div_max(divv, divi, ov, oi);
+  }
+  __shared__ double s_cv[BS / 32], s_dv[BS / 32];
+  __shared__ int s_ci[BS / 32], s_di[BS / 32];
+  __shared__ bool s_last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    s_cv[wid] = cflv;
+    s_ci[wid] = cfli;
+    s_dv[wid] = divv;
+    s_di[wid] = divi;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < BS / 32; w++) {
+      cfl_min(cflv, cfli, s_cv[w], s_ci[w]);
+      div_max(divv, divi, s_dv[w], s_di[w]);
+    }
+    F.red_v[2 * blockIdx.x] = cflv;
+    F.red_i[2 * blockIdx.x] = cfli;
+    F.red_v[2 * blockIdx.x + 1] = divv;
+    F.red_i[2 * blockIdx.x + 1] = divi;
+    __threadfence();
+    unsigned int t = atomicAdd(&S->ticket, 1u);
+    s_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!s_last) return;
+  // ---- last block: reduce the partials, then time_dr_end
+  __threadfence();
+  cflv = HUGE_VAL;
+  cfli = 0x7fffffff;
+  divv = DBL_MIN;
+  divi = -1;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += BS) {
+    cfl_min(cflv, cfli, ((volatile double*)F.red_v)[2 * b], ((volatile int*)F.red_i)[2 * b]);
+    div_max(divv, divi, ((volatile double*)F.red_v)[2 * b + 1], ((volatile int*)F.red_i)[2 * b + 1]);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    double ov = __shfl_xor_sync(0xffffffffu, cflv, o);
+    int oi = __shfl_xor_sync(0xffffffffu, cfli, o);
+    cfl_min(cflv, cfli, ov, oi);
+    ov = __shfl_xor_sync(0xffffffffu, divv, o);
+    oi = __shfl_xor_sync(0xffffffffu, divi, o);
+    div_max(divv, divi, ov, oi);
+  }
+  __syncthreads();
+  if (lane == 0) {
+    s_cv[wid] = cflv;
+    s_ci[wid] = cfli;
+    s_dv[wid] = divv;
+    s_di[wid] = divi;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  for (int w = 1; w < BS / 32; w++) {
+    cfl_min(cflv, cfli, s_cv[w], s_ci[w]);
+    div_max(divv, divi, s_dv[w], s_di[w]);
+  }
+  S->ticket = 0;
+  // time_dr_calc candidates then hydro's CFL and DIV (time_dr_advance.f90)
+  if (cflv < 0.0) {  // hydro_kn_getdtcfl FAILURE
+    S->ierr = -1;
+    S->iout = 2;
+    S->err_code = 1;
+    if (S->run_mode) S->halted = 1;
+    return;
+  }
+  const double rdt_cfl = C.cfl_sf * sqrt(cflv);
+  const double rdt_div = C.div_sf / divv;
+  S->cfl_rdt = rdt_cfl;
+  S->cfl_idt = cfli + 1;
+  S->div_rdt = rdt_div;
+  S->div_idt = divi + 1;
+  double mind = C.dt_max;
+  int mini = -1, mins = 0;
+  double g = C.dt_g * S->dt;
+  if (g < mind) { mind = g; mini = -1; mins = 1; }
+  if (S->nstep == 0 && C.dt_initial < mind) { mind = C.dt_initial; mini = -1; mins = 2; }
+  if (rdt_cfl < mind) { mind = rdt_cfl; mini = cfli + 1; mins = 3; }
+  if (rdt_div < mind) { mind = rdt_div; mini = divi + 1; mins = 4; }
+  S->nstep = S->nstep + 1;
+  S->dt = mind;
+  S->sdt = mins;
+  S->idtel = mini;
+  S->time = S->time + mind;
+  if (mind < C.dt_min) {
+    S->ierr = -1;
+    S->iout = 1;
+    S->err_code = 2;
+    if (S->run_mode) S->halted = 1;
+  }
+  if (S->run_mode) {
+    if (S->time >= C.time_end) S->stop_next = 1;
+    int r = S->nrecord;
+    if (F.hist && r < C.max_records) {
+      F.hist[r].time = S->time;
+      F.hist[r].dt = S->dt;
+      F.hist[r].nstep = S->nstep;
+      F.hist[r].idtel = S->idtel;
+      F.hist[r].sdt_code = S->sdt;
+      F.hist[r].ierr = S->ierr;
+    }
+    S->nrecord = r + 1;
+  }
+}
+
+// ================================================================ k_lag_force
+
+template <int BS>
+__global__ void __launch_bounds__(BS) k_lag_force(DevFields F, DevCfg C) {
+  const DevStep* S = F.step;
+  if (halted(S)) return;
+  const int iel = blockIdx.x * BS + threadIdx.x;
+  if (iel >= F.nel) return;
+  const double dt = S->dt;
+  const double hdt = 0.5 * dt;   // time_dr_setpredictor dts / getvertex step
+  const double zc = C.zerocut;
+  const int4 nd = __ldg(F.ielnd + iel);
+  const int n[4] = {nd.x, nd.y, nd.z, nd.w};
+  double x[4], y[4], u[4], v[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    x[j] = F.ndx[n[j]];
+    y[j] = F.ndy[n[j]];
+    u[j] = F.ndu[n[j]];
+    v[j] = F.ndv[n[j]];
+  }
+  const d4 qx = F.cnviscx[iel], qy = F.cnviscy[iel];
+  const int ireg = __ldg(F.ielreg + iel);
+  const int mat = __ldg(F.ielmat + iel);
+  const double m = F.mass[iel];
+  const double e0 = F.e[iel];
+  const int imx = F.elmx ? F.elmx[iel] : -1;
+  double fx[4], fy[4];
+  // ---- predictor force at t^n (hydro_dr_getforce, zcorrector false)
+  force_pq(F.p[iel], F.a1[iel], F.a3[iel], F.b1[iel], F.b3[iel], qx, qy, fx, fy);
+  if (C.zsp)
+    force_sp(__ldg(C.pmeritreg + ireg), F.rho[iel], F.cs2v[iel], x, y, F.spmass[iel], fx, fy);
+  // ---- half-step vertices (geometry_kn_getvertex with 0.5*dt)
+  double xh[4], yh[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    xh[j] = x[j] + hdt * u[j];
+    yh[j] = y[j] + hdt * v[j];
+  }
+  // ---- geometry, density (geometry_dr_getgeometry, density_dr_getdensity)
+  Iso g = getiso(xh, yh);
+  if (g.vol < 0.0) atomicMax(&F.step->negvol_pred, iel + 1);
+  const double rho = m / g.vol;
+  // ---- energy (hydro_kn_getenergy with dts = dt/2) and EoS
+  const double eh = energy_update(e0, m, zc, hdt, fx, fy, u, v);
+  double ph, cs2h;
+  eos_pc(C, mat, rho, eh, ph, cs2h);
+  // ---- mixed cells: component state at the half step
+  if (imx >= 0) {
+    const int c0 = F.imxfcp[imx], nc = F.imxncp[imx];
+    double ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0};
+    for (int k = 0; k < nc; k++) {
+      const int icp = c0 + k;
+      const double fr = F.frvol[icp];
+      // predictor component force with the t^n component state
+      double cfx[4], cfy[4];
+      force_pq(F.cpp[icp], F.a1[iel], F.a3[iel], F.b1[iel], F.b3[iel], F.cpviscx[icp],
+               F.cpviscy[icp], cfx, cfy);
+      // component energy with cpu = frvolume*cnu (utils_kn_mxgathercnav)
+      double cu[4], cv[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        cu[j] = fr * u[j];
+        cv[j] = fr * v[j];
+      }
+      const double cpm = F.cpm[icp];
+      const double cpe = energy_update(F.cpe[icp], cpm, zc, hdt, cfx, cfy, cu, cv);
+      F.cpe[icp] = cpe;  // the reference does not restore component energy
+      const double cpv = 4.0 * (g.a1 * g.b3 - g.a3 * g.b1) * fr;
+      const double cpr = cpm / cpv;
+      double cpp, cpc;
+      eos_pc(C, __ldg(F.icpmat + icp), cpr, cpe, cpp, cpc);
+      // corrector component force at the half-step state
+      force_pq(cpp, g.a1, g.a3, g.b1, g.b3, F.cpviscx[icp], F.cpviscy[icp], cfx, cfy);
+      F.cpfx[icp] = make_d4(cfx[0], cfx[1], cfx[2], cfx[3]);
+      F.cpfy[icp] = make_d4(cfy[0], cfy[1], cfy[2], cfy[3]);
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        ax[j] = ax[j] + fr * cfx[j];
+        ay[j] = ay[j] + fr * cfy[j];
+      }
+    }
+    // corrector element force: P+Q+SP+HG are overwritten by the average
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      fx[j] = ax[j];
+      fy[j] = ay[j];
+    }
+  } else {
+    // ---- corrector force at the half step (zcorrector true)
+    force_pq(ph, g.a1, g.a3, g.b1, g.b3, qx, qy, fx, fy);
+    if (C.zsp)
+      force_sp(__ldg(C.pmeritreg + ireg), rho, cs2h, xh, yh, F.spmass[iel], fx, fy);
+    if (C.zhg) force_hg(__ldg(C.kappareg + ireg), rho, g.vol, 1.0 / dt, u, v, fx, fy);
+  }
+  F.cnfx[iel] = make_d4(fx[0], fx[1], fx[2], fx[3]);
+  F.cnfy[iel] = make_d4(fy[0], fy[1], fy[2], fy[3]);
+  F.rho_h[iel] = rho;
+  F.cnwt_h[iel] = make_d4(g.w0, g.w1, g.w2, g.w3);
+}
+
+// ================================================================ k_lag_accel
+
+template <int BS>
+__global__ void __launch_bounds__(BS) k_lag_accel(DevFields F, DevCfg C) {
+  const DevStep* S = F.step;
+  if (halted(S)) return;
+  const int ind = blockIdx.x * BS + threadIdx.x;
+  if (ind >= F.nnd) return;
+  const double dt = S->dt;
+  const double zc = C.zerocut;
+  // hydro_kn_scatteracceleration: corner-major order over ielsort
+  double ndm = 0.0, nda = 0.0, fx = 0.0, fy = 0.0;
+  const int b = __ldg(F.nc_off + ind), e = __ldg(F.nc_off + ind + 1);
+  for (int k = b; k < e; k++) {
+    const int c = __ldg(F.nc_ent + k);
+    const int iel = c >> 2, jj = c & 3;
+    const double* cm = reinterpret_cast<const double*>(F.cnmass + iel);
+    const double cmj = cm[jj];
+    const double cw = reinterpret_cast<const double*>(F.cnwt_h + iel)[jj];
+    if (cmj > zc) {
+      ndm = ndm + cmj;
+    } else {
+      const double cmi = cm[(jj + 3) & 3];
+      if (cmi > zc) ndm = ndm + cmi;
+      else ndm = ndm + F.rho_h[iel] * cw;
+    }
+    nda = nda + cw;
+    fx = fx + reinterpret_cast<const double*>(F.cnfx + iel)[jj];
+    fy = fy + reinterpret_cast<const double*>(F.cnfy + iel)[jj];
+  }
+  // hydro_kn_getacceleration
+  const double w1 = C.dencut * nda;
+  double ax, ay;
+  if (ndm > w1) {
+    ax = fx / ndm;
+    ay = fy / ndm;
+  } else {
+    ax = 0.0;
+    ay = 0.0;
+  }
+  // utils_kn_bc on the accelerations
+  const int t = __ldg(F.indtype + ind);
+  if (t == -1) ax = 0.0;
+  else if (t == -2) ay = 0.0;
+  else if (t == -3) { ax = 0.0; ay = 0.0; }
+  const double w2 = ax * ax + ay * ay;
+  if (w2 < C.accut * C.accut) {
+    ax = 0.0;
+    ay = 0.0;
+  }
+  // hydro_kn_applyacceleration, then both half vertex moves
+  const double hdt = 0.5 * dt;
+  const double u0 = F.ndu[ind], v0 = F.ndv[ind];
+  const double u1 = u0 + dt * ax, v1 = v0 + dt * ay;
+  const double ub = u0 + hdt * ax, vb = v0 + hdt * ay;
+  double x = F.ndx[ind], y = F.ndy[ind];
+  x = x + hdt * u0;
+  y = y + hdt * v0;
+  x = x + hdt * u1;
+  y = y + hdt * v1;
+  F.ndu[ind] = u1;
+  F.ndv[ind] = v1;
+  F.ndubar[ind] = ub;
+  F.ndvbar[ind] = vb;
+  F.ndx[ind] = x;
+  F.ndy[ind] = y;
+}
+
+// ================================================================ k_lag_state
+
+template <int BS>
+__global__ void __launch_bounds__(BS) k_lag_state(DevFields F, DevCfg C) {
+  const DevStep* S = F.step;
+  if (halted(S)) return;
+  const int iel = blockIdx.x * BS + threadIdx.x;
+  if (iel >= F.nel) return;
+  const double dt = S->dt;
+  const double zc = C.zerocut;
+  const int4 nd = __ldg(F.ielnd + iel);
+  const int n[4] = {nd.x, nd.y, nd.z, nd.w};
+  double x[4], y[4], ub[4], vb[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    x[j] = F.ndx[n[j]];
+    y[j] = F.ndy[n[j]];
+    ub[j] = F.ndubar[n[j]];
+    vb[j] = F.ndvbar[n[j]];
+  }
+  Iso g = getiso(x, y);
+  if (g.vol < 0.0) atomicMax(&F.step->negvol_corr, iel + 1);
+  const double m = F.mass[iel];
+  const double rho = m / g.vol;
+  const d4 f4x = F.cnfx[iel], f4y = F.cnfy[iel];
+  const double fx[4] = {f4x.x, f4x.y, f4x.z, f4x.w};
+  const double fy[4] = {f4y.x, f4y.y, f4y.z, f4y.w};
+  const double e = energy_update(F.e[iel], m, zc, dt, fx, fy, ub, vb);
+  double p, cs2;
+  eos_pc(C, __ldg(F.ielmat + iel), rho, e, p, cs2);
+  F.a1[iel] = g.a1;
+  F.a2[iel] = g.a2;
+  F.a3[iel] = g.a3;
+  F.b1[iel] = g.b1;
+  F.b2[iel] = g.b2;
+  F.b3[iel] = g.b3;
+  F.cnwt[iel] = make_d4(g.w0, g.w1, g.w2, g.w3);
+  F.vol[iel] = g.vol;
+  F.rho[iel] = rho;
+  F.e[iel] = e;
+  F.p[iel] = p;
+  F.cs2[iel] = cs2;
+  const int imx = F.elmx ? F.elmx[iel] : -1;
+  if (imx >= 0) {
+    const int c0 = F.imxfcp[imx], nc = F.imxncp[imx];
+    for (int k = 0; k < nc; k++) {
+      const int icp = c0 + k;
+      const double fr = F.frvol[icp];
+      const d4 a = F.cpfx[icp], b = F.cpfy[icp];
+      const double cfx[4] = {a.x, a.y, a.z, a.w}, cfy[4] = {b.x, b.y, b.z, b.w};
+      double cu[4], cv[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        cu[j] = fr * ub[j];
+        cv[j] = fr * vb[j];
+      }
+      const double cpm = F.cpm[icp];
+      const double cpe = energy_update(F.cpe[icp], cpm, zc, dt, cfx, cfy, cu, cv);
+      const double cpv = 4.0 * (g.a1 * g.b3 - g.a3 * g.b1) * fr;
+      const double cpr = cpm / cpv;
+      double cpp, cpc;
+      eos_pc(C, __ldg(F.icpmat + icp), cpr, cpe, cpp, cpc);
+      F.cpe[icp] = cpe;
+      F.cpvol[icp] = cpv;
+      F.cprho[icp] = cpr;
+      F.cpp[icp] = cpp;
+      F.cpcs2[icp] = cpc;
+    }
+  }
+}
+
+// ================================================================ launchers
+
+static constexpr int BS_DT = 128;
+static constexpr int BS_EL = 128;
+static constexpr int BS_ND = 256;
+
+int getdt_blocks(int nel) { return (nel + BS_DT - 1) / BS_DT; }
+
+void launch_getdt(const DevFields& F, const DevCfg& C, cudaStream_t s) {
+  k_getdt<BS_DT><<<getdt_blocks(F.nel), BS_DT, 0, s>>>(F, C);
+}
+void launch_lag_force(const DevFields& F, const DevCfg& C, cudaStream_t s) {
+  k_lag_force<BS_EL><<<(F.nel + BS_EL - 1) / BS_EL, BS_EL, 0, s>>>(F, C);
+}
+void launch_lag_accel(const DevFields& F, const DevCfg& C, cudaStream_t s) {
+  k_lag_accel<BS_ND><<<(F.nnd + BS_ND - 1) / BS_ND, BS_ND, 0, s>>>(F, C);
+}
+void launch_lag_state(const DevFields& F, const DevCfg& C, cudaStream_t s) {
+  k_lag_state<BS_EL><<<(F.nel + BS_EL - 1) / BS_EL, BS_EL, 0, s>>>(F, C);
+}
+
+}  // namespace BL_NS
+}  // namespace bl

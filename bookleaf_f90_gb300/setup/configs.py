@@ -1,0 +1,212 @@
+"""The workloads, written as control files in the reference's namelist format.
+
+Each function returns the text of a deck that ``Problem.from_deck`` reads
+with the reference's own rules; the decks follow the reference's input/
+decks (sod_sm_lag_small, sedov_lag_small, noh_small) rescaled to the stated
+domains and mesh sizes:
+
+  sod(nx, ny)            Sod shock tube on [0,1]x[0,0.1], gamma 1.4, t=0.2
+  sod_reference(nx, ny)  the same problem in the reference check's geometry
+                         [0,100]x[0,10], t=20 (check_kn_tests.f90 applies)
+  sedov(n)               Sedov blast, quarter domain [0,1.2]^2, gamma 1.4,
+                         E=0.244816 in the corner cell, cold background 1e-12
+  noh(n, eulerian)       Noh implosion on [0,1]^2, gamma 5/3, u=-r/|r|
+"""
+
+
+def _mesh(nx, ny, x0, y0, x1, y1, bcs):
+    b, r, t, l = bcs
+    return f"""&MESH
+ region_typ(1)='LIN1'
+ region_dim(1,:)={nx},{ny}
+ region_side(1,1,:)=1,1
+ region_side(1,2,:)=1,2
+ region_side(1,3,:)=1,3
+ region_side(1,4,:)=1,4
+ segment_typ(:)='LINE','LINE','LINE','LINE'
+ segment_bc(:)='{b}','{r}','{t}','{l}'
+ segment_pos(1,:)={x0},{y0},{x1},{y0}
+ segment_pos(2,:)={x1},{y0},{x1},{y1}
+ segment_pos(3,:)={x1},{y1},{x0},{y1}
+ segment_pos(4,:)={x0},{y1},{x0},{y0}
+/
+"""
+
+
+def sod(nx=400, ny=40, time_end=0.2, eulerian=False, scale=1.0):
+    L = 1.0 * scale
+    H = 0.1 * scale
+    ale = "&ALE\n zeul=.TRUE.\n/\n" if eulerian else ""
+    s = scale
+    return f"""&CONTROL
+ time_start=0.0
+ time_end={time_end!r}
+ dt_initial={1.0e-5 * s!r}
+ dt_max={1.0e-3 * s!r}
+ dt_min={1.0e-10 * s!r}
+ dt_g=1.02
+ cfl_sf=0.5
+ cvisc1=0.5
+ cvisc2=0.75
+/
+&EOS
+ eos_type(1)='ideal gas'
+ eos_param(1,1)=1.4
+/
+""" + _mesh(nx, ny, 0.0, 0.0, L, H, ("SLIPY", "SLIPX", "SLIPY", "SLIPX")) + ale + f"""&INDICATORS
+ region_type(1)='background'
+ region_name(1)='air'
+ region_type(2)='shape'
+ region_name(2)='helium'
+ region_value(2)=1
+ material_type(1)='background'
+ material_name(1)='shocktube'
+/
+&INITIAL_CONDITIONS
+ thermodynamic_type(1)='region'
+ thermodynamic_value(1)=1
+ density(1)=1.0
+ energy(1)=2.5
+ thermodynamic_type(2)='region'
+ thermodynamic_value(2)=2
+ density(2)=0.125
+ energy(2)=2.0
+/
+&SHAPES
+ shape_type(1)='rectangle'
+ shape_param(1,:)={0.5 * L!r},{-0.1 * L!r},{1.5 * L!r},{0.5 * L!r}
+/
+"""
+
+
+def sod_reference(nx=100, ny=10, time_end=20.0, eulerian=False):
+    """Sod in the geometry the reference's known-answer check assumes."""
+    return sod(nx, ny, time_end=time_end, eulerian=eulerian, scale=100.0)
+
+
+def sedov(n=512, time_end=1.0, eulerian=False, gamma=1.4, energy=0.244816):
+    ale = "&ALE\n zeul=.TRUE.\n/\n" if eulerian else ""
+    return f"""&CONTROL
+ time_start=0.0
+ time_end={time_end!r}
+ dt_initial=1.0e-4
+ dt_max=1.0e-1
+ dt_min=1.0e-8
+ dt_g=1.02
+ cfl_sf=0.5
+ cvisc1=0.5
+ cvisc2=0.75
+/
+&EOS
+ eos_type(1)='ideal gas'
+ eos_param(1,1)={gamma!r}
+/
+""" + _mesh(n, n, 0.0, 0.0, 1.2, 1.2, ("SLIPY", "FREE", "FREE", "SLIPX")) + ale + f"""&INDICATORS
+ region_type(1)='background'
+ region_name(1)='air'
+ region_type(2)='cell'
+ region_name(2)='source'
+ region_value(2)=1
+ material_type(1)='background'
+ material_name(1)='air'
+/
+&INITIAL_CONDITIONS
+ thermodynamic_type(1)='region'
+ thermodynamic_value(1)=1
+ density(1)=1.0
+ energy(1)=1.0e-12
+ thermodynamic_type(2)='region'
+ thermodynamic_value(2)=2
+ thermodynamic_energy_scale(2)='volume'
+ density(2)=1.0
+ energy(2)={energy!r}
+/
+"""
+
+
+def noh(n=2048, time_end=0.6, eulerian=False):
+    ale = "&ALE\n zeul=.TRUE.\n/\n" if eulerian else ""
+    return f"""&CONTROL
+ time_start=0.0
+ time_end={time_end!r}
+ dt_initial=1.0e-4
+ dt_max=1.0e-2
+ dt_min=1.0e-8
+ dt_g=1.02
+ cfl_sf=0.5
+ cvisc1=0.5
+ cvisc2=0.75
+/
+&EOS
+ eos_type(1)='ideal gas'
+ eos_param(1,1)=1.6666667
+/
+&CUTOFF
+ zcut=1.0e-40
+ accut=1.0e-40
+ pcut=1.0e-40
+/
+""" + _mesh(n, n, 0.0, 0.0, 1.0, 1.0, ("SLIPY", "FREE", "FREE", "SLIPX")) + ale + """&INDICATORS
+ region_type(1)='background'
+ region_name(1)='air'
+ material_type(1)='background'
+ material_name(1)='air'
+/
+&INITIAL_CONDITIONS
+ thermodynamic_type(1)='region'
+ thermodynamic_value(1)=1
+ density(1)=1.0
+ energy(1)=0.0
+ kinematic_type(1)='background'
+ kinematic_value(1)=1
+ kinematic_geometry(1)='radial'
+ kinematic_param(1,1)=-1.0
+ kinematic_param(2:3,1)=0.0
+/
+"""
+
+
+def sod_multimaterial(nx=100, ny=25, time_end=20.0, vf=0.5):
+    """Two-material Sod with mixed cells, the reference's sod_mm_lag_small
+    set-up (material shape with a fixed volume fraction)."""
+    return f"""&CONTROL
+ time_start=0.0
+ time_end={time_end!r}
+ dt_initial=1.0e-3
+ dt_max=1.0e-1
+ dt_min=1.0e-8
+ dt_g=1.02
+ cfl_sf=0.5
+ cvisc1=0.5
+ cvisc2=0.75
+/
+&EOS
+ eos_type(1)='ideal gas'
+ eos_param(1,1)=1.4
+ eos_type(2)='ideal gas'
+ eos_param(1,2)=1.2
+/
+""" + _mesh(nx, ny, 0.0, 0.0, 100.0, 25.0, ("SLIPY", "SLIPX", "SLIPY", "SLIPX")) + f"""&INDICATORS
+ region_type(1)='background'
+ region_name(1)='shocktube'
+ material_type(1)='background'
+ material_name(1)='air'
+ material_type(2)='shape'
+ material_name(2)='helium'
+ material_value(2)=1
+/
+&INITIAL_CONDITIONS
+ thermodynamic_type(1)='region'
+ thermodynamic_value(1)=1
+ density(1)=1.0
+ energy(1)=2.5
+ thermodynamic_type(2)='material'
+ thermodynamic_value(2)=2
+ density(2)=0.125
+ energy(2)=2.0
+/
+&SHAPES
+ shape_type(1)='rectangle'
+ shape_param(1,:)=50.5,-10.0,150.0,50.0,{vf!r}
+/
+"""

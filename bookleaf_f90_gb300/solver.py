@@ -1,0 +1,111 @@
+"""Host-side mirror of the reference's solver interface for the hot path.
+
+``Solver`` is the Python counterpart of a Fortran host that calls the
+C-ABI: it registers a Problem's host arrays (like the reference's dh(:)),
+and exposes the three entry points under the reference's names
+
+    inf_solver_getdt   (src/infrastructure/solver/inf_solver_getdt.f90:35-70)
+    inf_solver_lagstep (src/infrastructure/solver/inf_solver_lagstep.f90:44-78)
+    inf_solver_alestep (src/infrastructure/solver/inf_solver_alestep.f90:39-74)
+
+with the reference's error behaviour: each returns error%ierr, and a
+non-zero return carries error%iout/serr in ``Solver.error`` (the Fortran
+wrapper would then call inf_error_halt).  ``run`` is the time loop of
+inf_control_solver (inf_control_solver.f90:53-69) executed on the device.
+"""
+import ctypes as ct
+
+import numpy as np
+
+from . import abi
+from ._lib import load
+
+
+class SolverError(RuntimeError):
+    def __init__(self, ierr, iout, message):
+        super().__init__("%s (ierr=%d, iout=%d)" % (message, ierr, iout))
+        self.ierr = ierr
+        self.iout = iout
+        self.message = message
+
+
+class Solver:
+    def __init__(self, problem, fp_mode=abi.FP_FAST):
+        self.L = load()
+        self.problem = problem
+        self.timestep = problem.timestep
+        self.error = abi.Error()
+        self._tab = problem.pointer_table()
+        self.ctx = ct.c_void_p()
+        ierr = self.L.bl_init(ct.byref(self.ctx), ct.byref(problem.sizes),
+                              ct.byref(problem.config), ct.cast(self._tab, ct.c_void_p),
+                              int(fp_mode), ct.byref(self.error))
+        if ierr != 0:
+            raise SolverError(ierr, self.error.iout, self.error.message)
+
+    # ---- the reference's entry points -------------------------------------
+    def inf_solver_getdt(self, ts=None):
+        return self.L.bl_getdt(self.ctx, ct.byref(ts or self.timestep), ct.byref(self.error))
+
+    def inf_solver_lagstep(self, ts=None):
+        return self.L.bl_lagstep(self.ctx, ct.byref(ts or self.timestep), ct.byref(self.error))
+
+    def inf_solver_alestep(self, ts=None):
+        return self.L.bl_alestep(self.ctx, ct.byref(ts or self.timestep), ct.byref(self.error))
+
+    def step(self, ts=None):
+        """One cycle of inf_control_solver's loop; returns error%ierr."""
+        ts = ts or self.timestep
+        for fn in (self.inf_solver_getdt, self.inf_solver_lagstep, self.inf_solver_alestep):
+            ierr = fn(ts)
+            if ierr != 0:
+                return ierr
+        return 0
+
+    def run(self, max_steps=10**9, ts=None, history=True):
+        """Device-resident time loop until time_end, max_steps or an error.
+        Returns (ierr, list of (nstep, time, dt, idtel, sdt))."""
+        ts = ts or self.timestep
+        max_steps = int(min(max_steps, 2**31 - 1))
+        hist = (abi.StepRecord * max_steps)() if history else None
+        n = ct.c_int(0)
+        ierr = self.L.bl_run(self.ctx, ct.byref(ts), max_steps,
+                             ct.cast(hist, ct.c_void_p) if history else None, ct.byref(n),
+                             ct.byref(self.error))
+        recs = []
+        if history:
+            for i in range(n.value):
+                r = hist[i]
+                recs.append((r.nstep, r.time, r.dt, r.idtel, abi.DT_NAMES[r.sdt_code]))
+        return ierr, recs
+
+    # ---- data movement ------------------------------------------------------
+    def sync_to_host(self, fid=0):
+        if self.L.bl_sync_to_host(self.ctx, int(fid)) != 0:
+            raise RuntimeError("bl_sync_to_host failed")
+
+    def sync_to_device(self, fid=0):
+        if self.L.bl_sync_to_device(self.ctx, int(fid)) != 0:
+            raise RuntimeError("bl_sync_to_device failed")
+
+    def synchronize(self):
+        return self.L.bl_synchronize(self.ctx)
+
+    @property
+    def stream(self):
+        return self.L.bl_stream(self.ctx)
+
+    @property
+    def kernel_launches(self):
+        return self.L.bl_kernel_launches(self.ctx)
+
+    def close(self):
+        if self.ctx:
+            self.L.bl_finalize(self.ctx)
+            self.ctx = ct.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,218 @@
+/*
+ * bookleaf_gb300.h -- C-ABI of the GB300 (sm_103a) hydro hot path.
+ *
+ * This library replaces BookLeaf's per-step solver entry points
+ *   inf_solver_getdt   (src/infrastructure/solver/inf_solver_getdt.f90:35-70)
+ *   inf_solver_lagstep (src/infrastructure/solver/inf_solver_lagstep.f90:44-78)
+ *   inf_solver_alestep (src/infrastructure/solver/inf_solver_alestep.f90:39-74)
+ * for a single-partition mesh.  The caller owns every field array for the
+ * whole run, exactly as BookLeaf's data_t handles do
+ * (src/dataAPI/dataAPI_types.f90:31-38, src/utilities/data/data.f90:129-304);
+ * the library keeps device mirrors and copies back on request.
+ *
+ * Conventions (all taken from the reference):
+ *  - Arrays are registered through a table of host pointers indexed by the
+ *    reference's dataAPI field IDs (src/dataAPI/dataAPI_id.f90:26-74), so a
+ *    Fortran host passes C_LOC(dh(id)%raddr(1)) / C_LOC(dh(id)%iaddr(1)).
+ *  - Corner and face arrays are Fortran (NCORN,nel) blocks: the four values
+ *    of one element are contiguous.
+ *  - Connectivity values are 1-based, as the Fortran host stores them.
+ *  - Every entry point returns error%ierr and fills bl_error like
+ *    error_t{ierr,iout,serr} (src/dataAPI/dataAPI_types.f90:76-79) with
+ *    SUCCESS=0, FAILURE=-1, HALT_ALL=1, HALT_SINGLE=2
+ *    (src/dataAPI/dataAPI_params.f90:31-34).  A negative volume returns
+ *    ierr = -iel of the offending element (geometry_kn_volume.f90:81-99).
+ *
+ * Nothing in these signatures is a torch or CUDA type: plain pointers,
+ * sizes and POD structs only.
+ */
+#ifndef BOOKLEAF_GB300_H
+#define BOOKLEAF_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- dataAPI field IDs (src/dataAPI/dataAPI_id.f90:26-74) ---------------- */
+enum {
+  BL_ELDENSITY = 1, BL_ELENERGY = 2, BL_ELPRESSURE = 3, BL_ELCS2 = 4,
+  BL_ELVOLUME = 5, BL_A1 = 6, BL_A2 = 7, BL_A3 = 8, BL_B1 = 9, BL_B2 = 10,
+  BL_B3 = 11, BL_CNWT = 12, BL_CNX = 13, BL_CNY = 14,
+  BL_RSCRATCH21 = 15, BL_RSCRATCH22 = 16, BL_RSCRATCH23 = 17,
+  BL_RSCRATCH24 = 18, BL_RSCRATCH25 = 19, BL_RSCRATCH26 = 20,
+  BL_RSCRATCH27 = 21, BL_RSCRATCH28 = 22,
+  BL_CNVISCX = 23, BL_CNVISCY = 24, BL_ELVISC = 25, BL_ELMASS = 26,
+  BL_CNMASS = 27,
+  BL_RSCRATCH11 = 28, BL_RSCRATCH12 = 29, BL_RSCRATCH13 = 30,
+  BL_RSCRATCH14 = 31, BL_RSCRATCH15 = 32, BL_RSCRATCH16 = 33,
+  BL_RSCRATCH17 = 34,
+  BL_NDX = 35, BL_NDY = 36, BL_NDU = 37, BL_NDV = 38, BL_INDTYPE = 39,
+  BL_IELSORT1 = 40, BL_IELND = 41, BL_IELEL = 42, BL_IELFC = 43,
+  BL_IELMAT = 44, BL_IELREG = 45, BL_IELSORT2 = 46, BL_SPMASS = 47,
+  BL_ISCRATCH11 = 48, BL_ZSCRATCH11 = 49, BL_IELLOCGLOB = 50,
+  BL_INDLOCGLOB = 51,
+  BL_CPDENSITY = 52, BL_CPENERGY = 53, BL_CPPRESSURE = 54, BL_CPCS2 = 55,
+  BL_CPVOLUME = 56, BL_FRVOLUME = 57, BL_CPMASS = 58, BL_FRMASS = 59,
+  BL_CPVISCX = 60, BL_CPVISCY = 61, BL_CPVISC = 62, BL_CPA1 = 63,
+  BL_CPA3 = 64, BL_CPB1 = 65, BL_CPB3 = 66, BL_ICPMAT = 67,
+  BL_ICPNEXT = 68, BL_ICPPREV = 69, BL_IMXEL = 70, BL_IMXFCP = 71,
+  BL_IMXNCP = 72, BL_ICPSCRATCH11 = 73, BL_ICPSCRATCH12 = 74,
+  BL_RCPSCRATCH11 = 75, BL_RCPSCRATCH21 = 76, BL_RCPSCRATCH22 = 77,
+  BL_RCPSCRATCH23 = 78, BL_RCPSCRATCH24 = 79,
+  BL_NID = 79
+};
+
+/* error_t codes (src/dataAPI/dataAPI_params.f90:31-34) */
+enum { BL_SUCCESS = 0, BL_FAILURE = -1, BL_HALT_ALL = 1, BL_HALT_SINGLE = 2 };
+
+/* Maximum materials / regions accepted (the reference's namelist bound LN). */
+#define BL_MAXMAT 100
+#define BL_MAXREG 100
+#define BL_NEOSPARAM 6
+#define BL_SLEN 130
+
+/* sizes_t (src/dataAPI/dataAPI_types.f90:40-43).  nel1=nel2=nel and
+ * nnd1=nnd2=nnd for one partition (init_kn.f90:108-119). */
+typedef struct {
+  int nel, nel1, nel2, nnd, nnd1, nnd2, nsz, nmat, nreg, ncp, nmx, mcp, mmx;
+} bl_sizes;
+
+/* The configuration scalars the hot path reads, flattened from config_t:
+ *   time_t   src/packages/time/config/time_types.f90:26-32
+ *   hydro_t  src/packages/hydro/config/hydro_types.f90:28-39
+ *   global_t src/utilities/data/global_types.f90 (zcut,zerocut,dencut,accut)
+ *   eos_t    src/utilities/eos/config/eos_types.f90:24-28, already
+ *            rationalised to materials 0..nmat (eos_config.f90:163-226)
+ *   ale_t    src/packages/ale/config/ale_types.f90:27-42
+ * Per-region arrays are indexed 0..nreg-1 for regions 1..nreg.  The EoS
+ * tables are indexed by material 0..nmat (material 0 = void). */
+typedef struct {
+  /* time_t */
+  double time_start, time_end, dt_g, dt_min, dt_max, dt_initial;
+  /* hydro_t */
+  double cvisc1, cvisc2, cfl_sf, div_sf;
+  int ztq, zhg, zsp, pad0;
+  double kappareg[BL_MAXREG], pmeritreg[BL_MAXREG];
+  int zdtnotreg[BL_MAXREG], zmidlength[BL_MAXREG];
+  /* global_t */
+  double zcut, zerocut, dencut, accut;
+  /* eos_t */
+  double ccut, pcut;
+  int eos_type[BL_MAXMAT + 1];
+  int pad1;
+  double eos_param[BL_MAXMAT + 1][BL_NEOSPARAM];
+  /* ale_t */
+  int ale_zexist, ale_zon, ale_zeul, ale_adv_type, ale_npatch, pad2;
+  double ale_mintime, ale_maxtime, ale_sf;
+} bl_config;
+
+/* timestep_t (src/dataAPI/dataAPI_types.f90:45-51).  mdt is reported as the
+ * material number imdt of the controlling element (>0), 0 for a mixed cell
+ * and -1 for none, because the library does not hold material names. */
+typedef struct {
+  double time, dt, dts;
+  int nstep, idtel, zcorrector, imdt;
+  char sdt[9];
+  char mdt[11];
+} bl_timestep;
+
+/* error_t (src/dataAPI/dataAPI_types.f90:76-79) */
+typedef struct {
+  int ierr, iout;
+  char serr[BL_SLEN + 1];
+} bl_error;
+
+/* Floating-point modes.  BL_FP_EXACT evaluates every expression in the
+ * reference's order without fused multiply-add, which reproduces a
+ * -ffp-contract=off CPU build bit for bit.  BL_FP_FAST lets the compiler
+ * contract a*b+c into one FMA (gfortran does the same at -O2 on aarch64);
+ * results then differ from the CPU build in the last bits. */
+enum { BL_FP_FAST = 0, BL_FP_EXACT = 1 };
+
+typedef struct bl_ctx bl_ctx;
+
+/* One row of the dt history written by bl_run (time_dr_end's mindt,
+ * src/packages/time/driver/time_dr_advance.f90:89-119). */
+typedef struct {
+  double time, dt;
+  int nstep, idtel, sdt_code, ierr;
+} bl_step_record;
+
+/* sdt codes used in bl_step_record, in time_dr_calc/hydro_dr_getdt order. */
+enum { BL_DT_MAXIMUM = 0, BL_DT_GROWTH = 1, BL_DT_INITIAL = 2, BL_DT_CFL = 3,
+       BL_DT_DIV = 4 };
+
+/* ---- lifetime ------------------------------------------------------------ */
+
+/* Allocates device mirrors and uploads every registered field.  Replaces the
+ * state the reference builds in inf_init (src/infrastructure/init/
+ * inf_init.F90:53-103): the caller has already generated the mesh, the
+ * connectivity ielel/ielfc, the node types, the initial state, the masses
+ * and (if zsp) spmass.  dh has BL_NID+1 entries; dh[0] is unused and dh[id]
+ * is the host array of field id (NULL for fields the path does not need:
+ * scratch, component arrays when ncp==0, spmass when zsp is false,
+ * ielsort2 when there is no ALE).  fp_mode is BL_FP_FAST or BL_FP_EXACT.
+ * The device ordinal is the current CUDA device of the calling thread. */
+int bl_init(bl_ctx **ctx, const bl_sizes *sizes, const bl_config *config,
+            void *const *dh, int fp_mode, bl_error *error);
+
+/* Frees every device allocation of the context. */
+int bl_finalize(bl_ctx *ctx);
+
+/* ---- the three solver entry points ------------------------------------- */
+
+/* inf_solver_getdt (inf_solver_getdt.f90:35-70): dt candidates
+ * (time_dr_calc), edge viscosity, elcs2 += elvisc, CFL and divergence
+ * limits, then time_dr_end (nstep+1, dt, time += dt, dt_min check).
+ * timestep is INOUT like runtime%timestep. */
+int bl_getdt(bl_ctx *ctx, bl_timestep *timestep, bl_error *error);
+
+/* inf_solver_lagstep (inf_solver_lagstep.f90:44-78): predictor and
+ * corrector.  Leaves timestep%zcorrector=1 and dts=dt like the reference. */
+int bl_lagstep(bl_ctx *ctx, bl_timestep *timestep, bl_error *error);
+
+/* inf_solver_alestep (inf_solver_alestep.f90:39-74): returns at once
+ * unless ale_active; otherwise flux volumes, advection and the hydro
+ * update (inf_solver_aleupdate.f90:34-56). */
+int bl_alestep(bl_ctx *ctx, const bl_timestep *timestep, bl_error *error);
+
+/* The reference's time loop (inf_control_solver.f90:53-69) run on the
+ * device: up to max_steps of getdt+lagstep+alestep, stopping after the step
+ * whose time reaches time_end (time_finish, time_dr_utils.f90:57-69) or on
+ * the first error.  dt selection and the end test happen on the device and
+ * the steps are replayed from CUDA graphs, so the host does not wait per
+ * step.  history (may be NULL) receives one record per step taken;
+ * *nsteps receives their number.  timestep is INOUT. */
+int bl_run(bl_ctx *ctx, bl_timestep *timestep, int max_steps,
+           bl_step_record *history, int *nsteps, bl_error *error);
+
+/* ---- data movement ------------------------------------------------------- */
+
+/* Copies device field id back into the host array registered for it (the
+ * reference's host readers: inf_io_output, check_dr_validate,
+ * hydro_dr_shortprint).  id = 0 copies every registered state field. */
+int bl_sync_to_host(bl_ctx *ctx, int id);
+
+/* Uploads host field id again after the host changed it (id = 0: all). */
+int bl_sync_to_device(bl_ctx *ctx, int id);
+
+/* ---- introspection ------------------------------------------------------- */
+
+/* Waits for the context's stream.  Returns 0 or a CUDA error number. */
+int bl_synchronize(bl_ctx *ctx);
+
+/* The cudaStream_t the context launches on, as an opaque pointer, for
+ * callers that time or order work against it. */
+void *bl_stream(bl_ctx *ctx);
+
+/* Number of kernels this context has launched so far. */
+long long bl_kernel_launches(bl_ctx *ctx);
+
+/* Library version string. */
+const char *bl_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BOOKLEAF_GB300_H */

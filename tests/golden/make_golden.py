@@ -1,0 +1,65 @@
+"""Write tests/golden/oracle_runs.json: regression fixtures of the CPU
+restatement (step count, time, dt, and exact checksums of the final fields)
+for small runs of each workload family.  The reference itself ships no
+golden vectors, so these pin the restatement against accidental change
+rather than against the reference.
+
+    python tests/golden/make_golden.py
+"""
+import json
+import os
+import struct
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from bookleaf_f90_gb300 import abi, configs  # noqa: E402
+
+CASES = {
+    "sod_lag_40x4": (configs.sod(40, 4), 60),
+    "sedov_lag_24": (configs.sedov(24), 60),
+    "noh_lag_24": (configs.noh(24), 40),
+    "noh_eul_24": (configs.noh(24, eulerian=True), 40),
+    "sod_mm_20x4": (configs.sod_multimaterial(20, 4), 40),
+}
+
+
+def _bits(a):
+    """Order-dependent exact checksum of a float64 array."""
+    import numpy as np
+    v = np.ascontiguousarray(a, dtype=np.float64).view(np.uint64)
+    h = np.uint64(1469598103934665603)
+    acc = 0
+    for chunk in np.array_split(v, max(1, v.size // 4096)):
+        acc = (acc * 1000003 + int(np.bitwise_xor.reduce(chunk * np.uint64(0x9E3779B97F4A7C15))
+                                   if chunk.size else 0)) % (1 << 61)
+    return "%016x" % ((acc ^ int(h)) & ((1 << 64) - 1))
+
+
+def summarise(p):
+    ts = p.timestep
+    out = {"nstep": ts.nstep, "time": struct.unpack("<Q", struct.pack("<d", ts.time))[0],
+           "dt": struct.unpack("<Q", struct.pack("<d", ts.dt))[0]}
+    for fid in (abi.ELDENSITY, abi.ELENERGY, abi.NDX, abi.NDY, abi.NDU, abi.NDV):
+        out[abi.NAMES[fid]] = _bits(p.fields[fid])
+    return out
+
+
+def main():
+    from bookleaf_f90_gb300 import Problem
+    from oracle.oracle import Oracle
+    res = {}
+    for name, (deck, steps) in CASES.items():
+        p = Problem.from_deck(deck)
+        o = Oracle(p)
+        ierr, n = o.run(p.timestep, steps)
+        assert ierr == 0
+        res[name] = summarise(p)
+        print(name, res[name]["nstep"])
+    with open(os.path.join(HERE, "oracle_runs.json"), "w") as f:
+        json.dump(res, f, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()

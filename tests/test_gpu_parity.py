@@ -1,0 +1,125 @@
+"""Parity of the sm_103a path with the CPU restatement, through the C-ABI.
+
+Exact mode (BL_FP_EXACT, no fused multiply-add) must reproduce the
+restatement bit for bit after every solver call.  Fast mode (FMA allowed)
+must stay within the stated tolerances of the reference's north-star
+criteria: total mass and energy to 1e-12 relative and density, energy and
+velocity fields within 1e-9 L1 relative.
+"""
+import numpy as np
+import pytest
+
+from bookleaf_f90_gb300 import Problem, Solver, abi, configs
+from helpers import compare, run_pair
+
+pytestmark = pytest.mark.gpu
+
+HG = configs.sedov(16).replace("cvisc2=0.75\n", "cvisc2=0.75\n kappaall=0.05\n pmeritall=0.3\n")
+DTNOT = configs.sod(24, 4).replace(
+    "cvisc2=0.75\n", "cvisc2=0.75\n zmidlength(2)=.TRUE.\n zdtnotreg(1)=.TRUE.\n")
+TENSOR = configs.sod(24, 4).replace("cvisc2=0.75\n", "cvisc2=0.75\n visc='TENSOR'\n")
+
+CASES = {
+    "sod_lag": (configs.sod(40, 6), 25),
+    "sod_ref_geometry": (configs.sod_reference(50, 5), 20),
+    "sedov_lag": (configs.sedov(24), 25),
+    "noh_lag": (configs.noh(24), 20),
+    "noh_eul": (configs.noh(24, eulerian=True), 20),
+    "sedov_eul": (configs.sedov(20, eulerian=True), 20),
+    "sod_eul": (configs.sod(40, 4, eulerian=True), 20),
+    "sod_multimaterial": (configs.sod_multimaterial(40, 10), 20),
+    "hourglass_subzonal": (HG, 20),
+    "dtnotreg_midlength": (DTNOT, 15),
+    "tensor_viscosity_off": (TENSOR, 10),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_exact_per_phase(name):
+    deck, n = CASES[name]
+    _, _, bad = run_pair(deck, n, exact=True, phases=True)
+    assert not bad, "\n".join(bad[:10])
+
+
+@pytest.mark.parametrize("name", ["sod_lag", "sedov_lag", "noh_eul", "sod_multimaterial"])
+def test_fast_within_tolerance(name):
+    deck, n = CASES[name]
+    pg, pc, bad = run_pair(deck, n, exact=False, phases=False, rtol=1e-9, atol=1e-12)
+    tg, tc = pg.totals(), pc.totals()
+    assert abs(tg["mass"] - tc["mass"]) <= 1e-12 * abs(tc["mass"])
+    et, ec = tg["ie"] + tg["ke"], tc["ie"] + tc["ke"]
+    assert abs(et - ec) <= 1e-12 * abs(ec)
+    for fid in (abi.ELDENSITY, abi.ELENERGY, abi.NDU, abi.NDV):
+        a, b = pg.fields[fid], pc.fields[fid]
+        l1 = np.sum(np.abs(a - b)) / max(np.sum(np.abs(b)), 1e-300)
+        assert l1 <= 1e-9, (abi.NAMES[fid], l1)
+
+
+def test_device_loop_matches_per_call():
+    """bl_run (device time loop, CUDA graphs) equals the per-call path."""
+    base = Problem.from_deck(configs.sedov(24, time_end=0.02))
+    pa, pb = base.copy(), base.copy()
+    sa = Solver(pa, fp_mode=abi.FP_EXACT)
+    steps = 0
+    while True:
+        assert sa.step() == 0
+        steps += 1
+        if pa.timestep.time >= pa.config.time_end:
+            break
+    sa.sync_to_host(0)
+    sb = Solver(pb, fp_mode=abi.FP_EXACT)
+    ierr, hist = sb.run()
+    assert ierr == 0, sb.error.message
+    sb.sync_to_host(0)
+    assert len(hist) == steps
+    assert pb.timestep.nstep == pa.timestep.nstep
+    assert pb.timestep.time == pa.timestep.time
+    assert not compare(pb, pa, exact=True)
+
+
+def test_device_loop_step_limit_and_resume():
+    base = Problem.from_deck(configs.noh(20, time_end=0.05, eulerian=True))
+    pa, pb = base.copy(), base.copy()
+    sa = Solver(pa, fp_mode=abi.FP_EXACT)
+    ierr, h1 = sa.run(max_steps=7)
+    assert ierr == 0 and len(h1) == 7
+    ierr, h2 = sa.run(max_steps=40)
+    assert ierr == 0
+    sa.sync_to_host(0)
+    sb = Solver(pb, fp_mode=abi.FP_EXACT)
+    for _ in range(7 + len(h2)):
+        assert sb.step() == 0
+    sb.sync_to_host(0)
+    assert not compare(pa, pb, exact=True)
+    assert [r[0] for r in h1 + h2] == list(range(1, 8 + len(h2)))
+
+
+def test_negative_volume_reports_element():
+    """A tangled mesh returns ierr = -iel of the last bad element with
+    HALT_SINGLE, like geometry_kn_checkvolume (fault made on the host)."""
+    from oracle.oracle import Oracle
+    p = Problem.from_deck(configs.sod(12, 3))
+    # move one interior node across its right-hand neighbour (nodes are
+    # numbered l + (k-1)*no_l with no_l = 4 here)
+    k = 7 * 4 + 2
+    p.fields[abi.NDX][k] += 2.5 * (1.0 / 12)
+    pc = p.copy()
+    s = Solver(p, fp_mode=abi.FP_EXACT)
+    o = Oracle(pc)
+    assert s.inf_solver_getdt() == o.getdt(pc.timestep)
+    eg = s.inf_solver_lagstep()
+    ec = o.lagstep(pc.timestep)
+    assert eg == ec and eg < 0
+    assert s.error.iout == abi.HALT_SINGLE
+    assert "negative volume" in s.error.message
+
+
+def test_dt_min_halt():
+    deck = configs.sod(16, 4).replace("dt_min=1e-10", "dt_min=0.5")
+    p = Problem.from_deck(deck)
+    s = Solver(p, fp_mode=abi.FP_EXACT)
+    ierr = s.inf_solver_getdt()
+    assert ierr == abi.FAILURE
+    assert s.error.iout == abi.HALT_ALL
+    assert s.error.message == "ERROR: dt < dt_min"
+    assert p.timestep.nstep == 1   # time_dr_end updates before the check

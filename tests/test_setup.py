@@ -1,0 +1,120 @@
+"""Host-side set-up: control-file reader, mesh, connectivity, node types,
+initial conditions (CPU only)."""
+import numpy as np
+import pytest
+
+from bookleaf_f90_gb300 import Problem, abi, configs
+from bookleaf_f90_gb300.setup import deck, mesh
+
+
+def test_namelist_sections_and_lists():
+    g = deck.parse("""&MESH
+ region_dim(1,:)=400,40
+ segment_typ(:)='LINE','LINE','LINE','LINE'
+ segment_pos(2,:)=1.0,0.0,1.0,0.1
+/
+&INITIAL_CONDITIONS
+ kinematic_param(1,1)=-1.0
+ kinematic_param(2:3,1)=0.0
+ density(2)=0.125   ! comment
+/
+""")
+    m = g["mesh"]
+    assert m["region_dim"][(1, 1)] == 400 and m["region_dim"][(1, 2)] == 40
+    assert [m["segment_typ"][(i,)] for i in range(1, 5)] == ["LINE"] * 4
+    assert m["segment_pos"][(2, 4)] == 0.1
+    ic = g["initial_conditions"]
+    assert ic["kinematic_param"][(2, 1)] == 0.0
+    assert (3, 1) not in ic["kinematic_param"]  # one value fills one element
+    assert ic["density"][(2,)] == 0.125
+
+
+def test_lin1_numbering_matches_reference_layout():
+    p = Problem.from_deck(configs.sod(8, 3))
+    nd = p.fields[abi.IELND]
+    # l (region_dim(:,2)) runs fastest: element 1 is the lower-left cell,
+    # corners counter-clockwise (setup_mesh.F90:1216-1225)
+    assert list(nd[0]) == [1, 5, 6, 2]
+    assert list(nd[1]) == [2, 6, 7, 3]
+    x, y = p.fields[abi.NDX], p.fields[abi.NDY]
+    # the corner is written last by side 4 (0.1 + 3*(-0.1)/3): -1.4e-17, as
+    # setup_mesh_line's arithmetic gives in the reference
+    assert x[0] == 0.0 and abs(y[0]) < 1e-16
+    assert y[3] == pytest.approx(0.1) and x[4] == pytest.approx(1 / 8)
+    assert np.all(p.fields[abi.ELVOLUME] > 0)
+    assert p.fields[abi.ELVOLUME].sum() == pytest.approx(0.1)
+
+
+def test_connectivity_is_symmetric():
+    p = Problem.from_deck(configs.sedov(7))
+    el, fc = p.fields[abi.IELEL], p.fields[abi.IELFC]
+    nel = p.nel
+    for iel in range(nel):
+        for j in range(4):
+            nb, f = el[iel, j] - 1, fc[iel, j] - 1
+            if nb == iel:
+                assert f == (j + 2) % 4    # boundary: self, opposite face
+            else:
+                assert el[nb, f] - 1 == iel and fc[nb, f] - 1 == j
+
+
+def test_node_types_and_corner_bc():
+    p = Problem.from_deck(configs.sod(6, 3))
+    t = p.fields[abi.INDTYPE]
+    # corners between a SLIPX and a SLIPY side become WALL (-3)
+    no_l = 4
+    corners = [0, no_l - 1, 6 * no_l, 7 * no_l - 1]
+    assert all(t[c] == -3 for c in corners)
+    assert np.all(t[[1, 2]] == -1)          # left edge SLIPX
+    assert t[no_l] == -2                    # bottom edge SLIPY
+    assert t[no_l + 1] == 1                 # interior: mesh region 1
+
+
+def test_sod_initial_state():
+    p = Problem.from_deck(configs.sod(10, 2))
+    rho, e = p.fields[abi.ELDENSITY], p.fields[abi.ELENERGY]
+    assert set(np.unique(rho)) == {1.0, 0.125}
+    assert np.all(p.fields[abi.ELPRESSURE][rho == 1.0] == pytest.approx(1.0))
+    assert np.all(p.fields[abi.ELPRESSURE][rho == 0.125] == pytest.approx(0.1))
+    assert p.config.zhg == 0 and p.config.zsp == 0
+
+
+def test_sedov_energy_deposit_and_noh_velocity():
+    p = Problem.from_deck(configs.sedov(16))
+    e, v = p.fields[abi.ELENERGY], p.fields[abi.ELVOLUME]
+    assert e[0] * v[0] == pytest.approx(0.244816)
+    assert e[1] == 1.0e-12
+    q = Problem.from_deck(configs.noh(8))
+    u, w = q.fields[abi.NDU], q.fields[abi.NDV]
+    assert u[0] == 0.0 and w[0] == 0.0           # origin, WALL corner
+    r = np.hypot(q.fields[abi.NDX], q.fields[abi.NDY])
+    inner = (q.fields[abi.INDTYPE] > 0)
+    assert np.allclose(np.hypot(u, w)[inner], 1.0)
+    assert np.all(u[inner] * q.fields[abi.NDX][inner] <= 0)
+    assert r.max() == pytest.approx(np.sqrt(2))
+
+
+def test_multimaterial_components():
+    p = Problem.from_deck(configs.sod_multimaterial(20, 4))
+    s = p.sizes
+    assert s.nmx == 4 and s.ncp == 8               # one column of mixed cells
+    assert np.all(p.fields[abi.IELMAT][p.fields[abi.IMXEL] - 1] < 0)
+    fr = p.fields[abi.FRVOLUME]
+    assert np.allclose(fr, 0.5)
+    assert list(p.fields[abi.ICPMAT][:2]) == [1, 2]
+
+
+def test_reference_decks_parse():
+    import glob
+    import os
+    decks = sorted(glob.glob("/root/reference/input/*"))
+    if not decks:
+        pytest.skip("reference decks not present")
+    for d in decks:
+        text = open(d).read()
+        if "ARC_" in text:
+            with pytest.raises(deck.DeckError):
+                Problem.from_deck(text)
+            continue
+        p = Problem.from_deck(text)
+        assert p.nel > 0 and np.all(p.fields[abi.ELVOLUME] > 0), os.path.basename(d)
