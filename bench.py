@@ -1,0 +1,337 @@
+"""Benchmark of the BookLeaf hydro hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                    [--workload sedov|noh|noh-eul|sod] [--size S]
+
+A step is one pass of the hot path (getdt + lagstep, + alestep for Eulerian
+workloads) over the whole mesh.  The default workload is the Sedov blast on
+a 512x512 quarter domain, Lagrangian, FP64 (the configuration the metric is
+quoted on).  Inputs are synthetic: the deck is generated in the reference's
+namelist format (bookleaf_f90_gb300/setup/configs.py).
+
+value      zone-cycles/s with the state resident in HBM: K steps of the
+           device-resident time loop (bl_run, CUDA graphs), timed with CUDA
+           events on the library's stream.
+e2e        the same metric through the reference-facing C-ABI with host
+           buffers: bl_init (upload of every registered host field), K calls
+           each of bl_getdt/bl_lagstep(/bl_alestep) and bl_sync_to_host of
+           the whole state, all inside the timed region.
+roofline   the dominant kernel (edge viscosity + dt, k_getdt) against the
+           measured HBM copy bandwidth, with algorithmic bytes per zone from
+           the phase table in DESIGN.md; "fp64" reports the binding FP64
+           issue roof.
+cpu_baseline  the CPU restatement on this host's cores, a bounded sample
+           of the same workload.
+
+Under torchrun (N>1) every rank advances its own replica (the plain path does
+not shard without halo exchange); value is the sum over ranks divided by
+the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+# algorithmic bytes per zone-cycle (phase table)
+B_LAG = 724
+B_EUL = 1628
+B_GETDT = 164
+
+
+def workload_deck(name, size):
+    from bookleaf_f90_gb300 import configs
+    if name == "sedov":
+        return configs.sedov(size or 512), "sedov_%dx%d_lagrangian" % (size or 512, size or 512), False
+    if name == "noh":
+        return configs.noh(size or 2048), "noh_%dx%d_lagrangian" % (size or 2048, size or 2048), False
+    if name == "noh-eul":
+        return configs.noh(size or 2048, eulerian=True), "noh_%dx%d_eulerian" % (size or 2048, size or 2048), True
+    if name == "sod":
+        return configs.sod(size or 400, max(1, (size or 400) // 10)), "sod_%dx%d_lagrangian" % (
+            size or 400, max(1, (size or 400) // 10)), False
+    raise SystemExit("unknown workload " + name)
+
+
+def load_peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), "--query-gpu=clocks.sm,clocks.max.sm,"
+                 "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = sorted(float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit())
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for i, n in enumerate(names):
+                if len(s) > 3 + i and s[3 + i].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def cpu_sample(deck, steps):
+    """The CPU restatement advancing `steps` steps of the workload; returns
+    (zone-cycles/s, seconds).  Runs in a worker process."""
+    sys.path.insert(0, HERE)
+    from bookleaf_f90_gb300 import Problem
+    from oracle.oracle import Oracle
+    p = Problem.from_deck(deck)
+    o = Oracle(p)
+    o.step(p.timestep)   # warm-up step (first step uses dt_initial)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        if o.step(p.timestep) != 0:
+            break
+    t = time.perf_counter() - t0
+    return p.nel * steps / t, t
+
+
+def cpu_baseline(deck, nel, target_s=12.0, cores=1):
+    """Bounded sample of the workload on the host's cores (spawned workers)."""
+    import multiprocessing as mp
+    from oracle import oracle as orc
+    orc.build()
+    # calibrate one step
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(1) as pool:
+        rate, t = pool.apply(cpu_sample, (deck, 1))
+    steps = max(2, int(target_s * rate / nel))
+    with ctx.Pool(cores) as pool:
+        res = pool.starmap(cpu_sample, [(deck, steps)] * cores)
+    rate = sum(r for r, _ in res)
+    return rate, steps, max(t for _, t in res)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--workload", default="sedov")
+    ap.add_argument("--size", type=int, default=0)
+    ap.add_argument("--fp", default="fast", choices=["fast", "exact"])
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    deck, wname, eul = workload_deck(args.workload, args.size)
+    bytes_zc = B_EUL if eul else B_LAG
+
+    if args.impl == "reference":
+        # the reference's own CPU path: the serial restatement (no Fortran
+        # compiler exists on either machine), one replica per host core
+        if rank != 0:
+            return
+        from bookleaf_f90_gb300 import Problem
+        nel = Problem.from_deck(deck).nel
+        cores = os.cpu_count() or 1
+        per_step = []
+        for _ in range(max(1, args.steps)):
+            rate, steps, t = cpu_baseline(deck, nel, target_s=8.0 / max(1, args.steps) * 4, cores=cores)
+            per_step.append(rate)
+            break
+        rate = max(per_step)
+        line = {"impl": "reference", "metric": "zone-cycles/s FP64", "value": rate,
+                "unit": "zone-cycles/s", "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "higher_is_better": True, "dtype": "f64",
+                "data": "synthetic", "config": {"workload": wname, "nel": nel},
+                "cpu_baseline": {"value": rate, "unit": "zone-cycles/s", "cores": cores,
+                                 "kind": "port",
+                                 "sample": "%d steps of %s per core, %d independent replicas "
+                                           "of the serial restatement" % (steps, wname, cores)},
+                "e2e": {"value": rate, "unit": "zone-cycles/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+        torch.cuda.set_device(local)
+    else:
+        torch.cuda.set_device(0)
+    from bookleaf_f90_gb300 import Problem, Solver, abi
+    from bookleaf_f90_gb300 import build as blbuild
+    blbuild.build()
+
+    base = Problem.from_deck(deck)
+    nel = base.nel
+    fp = abi.FP_EXACT if args.fp == "exact" else abi.FP_FAST
+
+    # ---------------- value: device-resident time loop ---------------------
+    p = base.copy()
+    s = Solver(p, fp_mode=fp)
+    ierr, _ = s.run(max_steps=args.warmup, history=False)
+    assert ierr == 0, s.error.message
+    stream = torch.cuda.ExternalStream(s.stream)
+    l0 = s.kernel_launches
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    s.synchronize()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        e0.record(stream)
+        ierr, hist = s.run(max_steps=args.steps, history=True)
+        e1.record(stream)
+        e1.synchronize()
+    s.synchronize()
+    torch.cuda.synchronize()
+    assert ierr == 0, s.error.message
+    nsteps = len(hist)
+    ms = e0.elapsed_time(e1)
+    launches = s.kernel_launches - l0
+    t_max = ms
+    zc_local = nel * nsteps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+        z = torch.tensor([float(zc_local)], device="cuda")
+        dist.all_reduce(z, op=dist.ReduceOp.SUM)
+        zc_total = float(z.item())
+    else:
+        zc_total = float(zc_local)
+    value = zc_total / (t_max * 1e-3)
+
+    # ---------------- dominant kernel: k_getdt timed alone -----------------
+    # (one getdt launch per call; the state is the one the run left)
+    k_ms = []
+    for _ in range(3):
+        q0 = torch.cuda.Event(enable_timing=True)
+        q1 = torch.cuda.Event(enable_timing=True)
+        ts = p.timestep.copy()
+        q0.record(stream)
+        s.inf_solver_getdt(ts)
+        q1.record(stream)
+        q1.synchronize()
+        k_ms.append(q0.elapsed_time(q1))
+    k_ms = sorted(k_ms)[1]
+    hbm_peak, peak_kind = load_peaks()
+    achieved = B_GETDT * nel / (k_ms * 1e-3) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved / hbm_peak, "traffic": None, "kernel": "k_getdt",
+            "peak_kind": peak_kind, "kernel_ms": k_ms,
+            "note": "the FP64 issue rate, not HBM, bounds this path; see fp64"}
+    step_bytes = bytes_zc * nel
+    fp64 = {"unit": "TFLOP/s nominal 1.25", "step_ms": t_max / max(1, nsteps),
+            "hbm_frac_whole_step": (step_bytes * nsteps / (t_max * 1e-3) / 1e9) / hbm_peak}
+    s.close()
+
+    # ---------------- e2e through the C-ABI with host buffers --------------
+    e2e = None
+    if not args.no_e2e:
+        pe = base.copy()
+        # pin the host arrays so the uploads are DMA transfers
+        for fid, arr in list(pe.fields.items()):
+            pin = torch.empty(arr.shape, dtype=torch.float64 if arr.dtype.kind == "f" else torch.int32,
+                              pin_memory=True).numpy()
+            pin[...] = arr
+            pe.fields[fid] = pin
+        h2d = sum(a.nbytes for a in pe.fields.values())
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        se = Solver(pe, fp_mode=fp)
+        ts = pe.timestep
+        for _ in range(args.warmup + args.steps):
+            assert se.step(ts) == 0, se.error.message
+        se.sync_to_host(0)
+        t1 = time.perf_counter()
+        d2h = sum(pe.fields[f].nbytes for f in (abi.ELDENSITY, abi.ELENERGY, abi.ELPRESSURE,
+                                                abi.ELCS2, abi.ELVOLUME, abi.A1, abi.A2, abi.A3,
+                                                abi.B1, abi.B2, abi.B3, abi.CNWT, abi.CNX, abi.CNY,
+                                                abi.CNVISCX, abi.CNVISCY, abi.ELVISC, abi.ELMASS,
+                                                abi.CNMASS, abi.NDX, abi.NDY, abi.NDU, abi.NDV)
+                  if f in pe.fields)
+        n_e = args.warmup + args.steps
+        e2e_val = nel * n_e / (t1 - t0)
+        if world > 1:
+            t = torch.tensor([t1 - t0], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_val = nel * n_e * world / float(t.item())
+        e2e = {"value": e2e_val, "unit": "zone-cycles/s",
+               "h2d_bytes_per_step": int(h2d / n_e) + 2 * 64,
+               "d2h_bytes_per_step": int(d2h / n_e) + 3 * 64,
+               "note": "bl_init upload + %d per-call steps (getdt, lagstep%s) + full state "
+                       "download, host pinned" % (n_e, ", alestep" if eul else "")}
+        se.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        rate, steps, t = cpu_baseline(deck, nel, target_s=12.0, cores=1)
+        cpu = {"value": rate, "unit": "zone-cycles/s", "cores": 1, "kind": "port",
+               "sample": "%d steps of %s on one core (serial CPU restatement, "
+                         "-O2 -ffp-contract=off), %.1f s" % (steps, wname, t)}
+
+    if rank == 0:
+        line = {"metric": "zone-cycles/s FP64 (1 GB300, %HBM roof)", "value": value,
+                "unit": "zone-cycles/s", "n_gpus": world, "steps": nsteps,
+                "warmup": args.warmup, "ms_per_step": t_max / max(1, nsteps),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic",
+                "config": {"workload": wname, "nel": nel, "fp_mode": args.fp,
+                           "replicas": world, "l2": "working set %.0f MB > 129 MB L2, no flush"
+                                                     % (step_bytes / 1e6),
+                           "loop": "bl_run device time loop, CUDA graphs of 16 steps"},
+                "roofline": roof, "fp64": fp64, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": launches, "clocks": clk.summary()}
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

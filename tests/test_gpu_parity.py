@@ -49,10 +49,14 @@ def test_fast_within_tolerance(name):
     assert abs(tg["mass"] - tc["mass"]) <= 1e-12 * abs(tc["mass"])
     et, ec = tg["ie"] + tg["ke"], tc["ie"] + tc["ke"]
     assert abs(et - ec) <= 1e-12 * abs(ec)
-    for fid in (abi.ELDENSITY, abi.ELENERGY, abi.NDU, abi.NDV):
+    for fid in (abi.ELDENSITY, abi.ELENERGY):
         a, b = pg.fields[fid], pc.fields[fid]
         l1 = np.sum(np.abs(a - b)) / max(np.sum(np.abs(b)), 1e-300)
         assert l1 <= 1e-9, (abi.NAMES[fid], l1)
+    # the velocity field as a whole (in Sod the y component is round-off)
+    du = np.abs(pg.fields[abi.NDU] - pc.fields[abi.NDU]) + np.abs(pg.fields[abi.NDV] - pc.fields[abi.NDV])
+    un = np.abs(pc.fields[abi.NDU]) + np.abs(pc.fields[abi.NDV])
+    assert np.sum(du) <= 1e-9 * np.sum(un), np.sum(du) / np.sum(un)
 
 
 def test_device_loop_matches_per_call():
@@ -115,7 +119,8 @@ def test_negative_volume_reports_element():
 
 
 def test_dt_min_halt():
-    deck = configs.sod(16, 4).replace("dt_min=1e-10", "dt_min=0.5")
+    deck = configs.sod(16, 4).replace("dt_min=1e-10", "dt_min=0.5").replace(
+        "dt_max=0.001", "dt_max=1.0")
     p = Problem.from_deck(deck)
     s = Solver(p, fp_mode=abi.FP_EXACT)
     ierr = s.inf_solver_getdt()
