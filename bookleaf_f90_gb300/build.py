@@ -18,7 +18,6 @@ OUTDIR = os.path.join(HERE, "_lib")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(OUTDIR, "libbookleaf_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-HEADERS = ["bl_device.cuh", "bl_kernels.h", "hydro_kernels.cuh", "ale_kernels.cuh"]
 
 
 def nvcc():
@@ -49,6 +48,8 @@ def build(force=False, verbose=False, extra=()):
         (common + ["--fmad=false", "-DBL_NS=exact", "-c", os.path.join(CSRC, "bl_kernels.cu"),
                    "-o", os.path.join(BUILD, "k_exact.o")]),
         (common + ["-c", os.path.join(CSRC, "bl_capi.cu"), "-o", os.path.join(BUILD, "capi.o")]),
+        (common + ["--fmad=true", "-c", os.path.join(CSRC, "bl_noalloc.cu"),
+                   "-o", os.path.join(BUILD, "noalloc.o")]),
     ]
     procs = [subprocess.Popen(j, stdout=subprocess.PIPE, stderr=subprocess.STDOUT) for j in jobs]
     logs = []
@@ -62,7 +63,8 @@ def build(force=False, verbose=False, extra=()):
     subprocess.check_call([cc] + ARCH + ["-shared", "-cudart", "static", "-o", tmp,
                                          os.path.join(BUILD, "k_fast.o"),
                                          os.path.join(BUILD, "k_exact.o"),
-                                         os.path.join(BUILD, "capi.o")])
+                                         os.path.join(BUILD, "capi.o"),
+                                         os.path.join(BUILD, "noalloc.o")])
     os.replace(tmp, LIB)
     if verbose:
         sys.stdout.write("\n".join(logs))

@@ -211,6 +211,47 @@ long long bl_kernel_launches(bl_ctx *ctx);
 /* Library version string. */
 const char *bl_version(void);
 
+/* ---- allocation-free getdt ---------------------------------------------- */
+
+/* Largest mesh bl_getdt_noalloc accepts: its reduction scratch lives in a
+ * fixed 1.5 MiB device array (65,536 blocks of 128 elements). */
+#define BL_NOALLOC_MAX_NEL (65536 * 128)
+
+/* Device arrays for bl_getdt_noalloc, in the reference's own layout: every
+ * pointer is device memory the caller owns; connectivity is 1-based;
+ * corner/face arrays are (NCORN,nel) blocks.  Pure-material meshes only
+ * (no mixed cells). */
+typedef struct {
+  int nel, nnd;
+  const double *ndx, *ndy, *ndu, *ndv;           /* [nnd] */
+  const int *indtype;                            /* [nnd] */
+  const int *ielnd, *ielel, *ielfc;              /* [4*nel], 1-based */
+  const int *ielreg;                             /* [nel], 1-based */
+  const double *eldensity, *elcs2;               /* [nel] inputs */
+  const double *a1, *a3, *b1, *b3, *elvolume;    /* [nel] inputs */
+  double *cnviscx, *cnviscy;                     /* [4*nel] outputs */
+  double *elvisc;                                /* [nel] output */
+  double *elcs2_out;                             /* [nel] output: elcs2+elvisc */
+} bl_getdt_arrays;
+
+/* No counterpart in the reference: an allocation-free variant of bl_getdt
+ * for callers that cannot call cudaMalloc -- for example a host that hands
+ * out all device memory from its own pool, or code running where a device
+ * allocation would break a captured sequence of work.  It runs the same
+ * computation as bl_getdt (edge viscosity, elcs2+elvisc, CFL and divergence
+ * limits, time_dr_calc/time_dr_end) on arrays the caller passes, without a
+ * bl_ctx.  Its reduction scratch is a fixed file-scope device array, held by
+ * every GPU that loads the library until the process exits; nothing is
+ * allocated or freed by this call.  The first call on a device looks up that
+ * array's device address (cudaGetSymbolAddress); make that first call
+ * before any stream capture.  Calls that overlap on the GPU (other streams,
+ * other host threads) share the array and race: serialise them.  Returns
+ * the reference's error codes like bl_getdt; nel > BL_NOALLOC_MAX_NEL is
+ * rejected with FAILURE.  stream is a cudaStream_t (NULL: the legacy
+ * default stream); the call waits for it before returning timestep. */
+int bl_getdt_noalloc(const bl_getdt_arrays *arrays, const bl_config *config,
+                     bl_timestep *timestep, void *stream, bl_error *error);
+
 #ifdef __cplusplus
 }
 #endif
