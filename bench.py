@@ -29,6 +29,8 @@ the slowest rank's time.
 """
 import argparse
 import json
+
+import numpy as np
 import os
 import subprocess
 import sys
@@ -42,12 +44,20 @@ sys.path.insert(0, HERE)
 B_LAG = 724
 B_EUL = 1628
 B_GETDT = 164
+# FP64-pipe instructions (DFMA+DMUL+DADD+DSETP) k_getdt executes per zone on
+# the default workload, from the ncu opcode counts of the committed capture
+# (profiles/k_getdt_sedov512.md); with the FMA rate measured live below they
+# place k_getdt against the FP64 issue roof that binds it.
+FP64_PER_ZONE_GETDT = 937
 
 
 def workload_deck(name, size):
     from bookleaf_f90_gb300 import configs
     if name == "sedov":
-        return configs.sedov(size or 512), "sedov_%dx%d_lagrangian" % (size or 512, size or 512), False
+        # the reference's Sedov decks set the hourglass filter kappaall=0.01
+        # (input/sedov_lag_small); without it the run cannot reach t = 1
+        n = size or 512
+        return configs.sedov(n, kappa=0.01), "sedov_%dx%d_lagrangian_hg0.01" % (n, n), False
     if name == "noh":
         return configs.noh(size or 2048), "noh_%dx%d_lagrangian" % (size or 2048, size or 2048), False
     if name == "noh-eul":
@@ -152,7 +162,8 @@ def cpu_baseline(deck, nel, target_s=12.0, cores=1):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=0,
+                    help="timed steps; 0 (default) runs the workload to its end time")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--workload", default="sedov")
@@ -169,27 +180,27 @@ def main():
     bytes_zc = B_EUL if eul else B_LAG
 
     if args.impl == "reference":
-        # the reference's own CPU path: the serial restatement (no Fortran
-        # compiler exists on either machine), one replica per host core
+        # The reference's CPU implementation of the path on the host cores.
+        # No Fortran compiler exists on either machine, so the reference
+        # itself cannot be built; its C restatement (oracle/, -O2, no FMA
+        # contraction) stands in.  One independent replica per host core,
+        # as the reference's MPI ranks each run the serial loop over their
+        # partition.  Under torchrun only rank 0 runs.
         if rank != 0:
             return
         from bookleaf_f90_gb300 import Problem
         nel = Problem.from_deck(deck).nel
         cores = os.cpu_count() or 1
-        per_step = []
-        for _ in range(max(1, args.steps)):
-            rate, steps, t = cpu_baseline(deck, nel, target_s=8.0 / max(1, args.steps) * 4, cores=cores)
-            per_step.append(rate)
-            break
-        rate = max(per_step)
+        rate, steps, t = cpu_baseline(deck, nel, target_s=20.0, cores=cores)
         line = {"impl": "reference", "metric": "zone-cycles/s FP64", "value": rate,
                 "unit": "zone-cycles/s", "n_gpus": args.gpus, "steps": args.steps,
                 "warmup": args.warmup, "higher_is_better": True, "dtype": "f64",
                 "data": "synthetic", "config": {"workload": wname, "nel": nel},
                 "cpu_baseline": {"value": rate, "unit": "zone-cycles/s", "cores": cores,
                                  "kind": "port",
-                                 "sample": "%d steps of %s per core, %d independent replicas "
-                                           "of the serial restatement" % (steps, wname, cores)},
+                                 "sample": "%d steps of %s on each of %d cores (independent "
+                                           "replicas of the serial CPU restatement), %.1f s"
+                                           % (steps, wname, cores, t)},
                 "e2e": {"value": rate, "unit": "zone-cycles/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
@@ -204,6 +215,7 @@ def main():
         torch.cuda.set_device(0)
     from bookleaf_f90_gb300 import Problem, Solver, abi
     from bookleaf_f90_gb300 import build as blbuild
+    from bookleaf_f90_gb300.replicas import job_rate
     blbuild.build()
 
     base = Problem.from_deck(deck)
@@ -211,10 +223,19 @@ def main():
     fp = abi.FP_EXACT if args.fp == "exact" else abi.FP_FAST
 
     # ---------------- value: device-resident time loop ---------------------
+    # W warm-up steps (graph capture, caches), then the initial state is
+    # uploaded again and the timed run starts at t = 0: K steps, or with
+    # K = 0 the whole run to time_end (the configuration's own end time).
     p = base.copy()
     s = Solver(p, fp_mode=fp)
-    ierr, _ = s.run(max_steps=args.warmup, history=False)
+    init = {fid: arr.copy() for fid, arr in p.fields.items()}
+    ts0 = p.timestep.copy()
+    ierr, _ = s.run(max_steps=max(1, args.warmup), ts=p.timestep.copy(), history=False)
     assert ierr == 0, s.error.message
+    for fid, arr in init.items():
+        np.copyto(p.fields[fid], arr)
+    s.sync_to_device(0)
+    ts = ts0.copy()
     stream = torch.cuda.ExternalStream(s.stream)
     l0 = s.kernel_launches
     e0 = torch.cuda.Event(enable_timing=True)
@@ -225,27 +246,18 @@ def main():
     s.synchronize()
     with ClockSampler(torch.cuda.current_device()) as clk:
         e0.record(stream)
-        ierr, hist = s.run(max_steps=args.steps, history=True)
+        ierr, _ = s.run(max_steps=args.steps if args.steps > 0 else 10**9, ts=ts, history=False)
         e1.record(stream)
         e1.synchronize()
     s.synchronize()
     torch.cuda.synchronize()
     assert ierr == 0, s.error.message
-    nsteps = len(hist)
+    nsteps = ts.nstep - ts0.nstep
+    t_end = ts.time
     ms = e0.elapsed_time(e1)
     launches = s.kernel_launches - l0
-    t_max = ms
-    zc_local = nel * nsteps
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-        z = torch.tensor([float(zc_local)], device="cuda")
-        dist.all_reduce(z, op=dist.ReduceOp.SUM)
-        zc_total = float(z.item())
-    else:
-        zc_total = float(zc_local)
-    value = zc_total / (t_max * 1e-3)
+    value, t_max, _ = job_rate(ms, nel * nsteps, device="cuda")
+    p.timestep = ts
 
     # ---------------- dominant kernel: k_getdt timed alone -----------------
     # (one getdt launch per call; the state is the one the run left)
@@ -267,7 +279,14 @@ def main():
             "peak_kind": peak_kind, "kernel_ms": k_ms,
             "note": "the FP64 issue rate, not HBM, bounds this path; see fp64"}
     step_bytes = bytes_zc * nel
-    fp64 = {"unit": "TFLOP/s nominal 1.25", "step_ms": t_max / max(1, nsteps),
+    from bookleaf_f90_gb300 import _lib
+    rates = _lib.fp64_rates()
+    fp64_ach = FP64_PER_ZONE_GETDT * nel / (k_ms * 1e-3) / 1e9
+    fp64 = {"bound": "fp64", "kernel": "k_getdt", "unit": "G FP64-pipe instr/s",
+            "achieved": fp64_ach, "peak": rates["dfma"], "frac": fp64_ach / rates["dfma"],
+            "peak_kind": "measured live (DFMA issue loop, bl_fp64_rates)",
+            "instr_per_zone": FP64_PER_ZONE_GETDT, "rates_gops": rates,
+            "step_ms": t_max / max(1, nsteps),
             "hbm_frac_whole_step": (step_bytes * nsteps / (t_max * 1e-3) / 1e9) / hbm_peak}
     s.close()
 
@@ -286,8 +305,10 @@ def main():
         t0 = time.perf_counter()
         se = Solver(pe, fp_mode=fp)
         ts = pe.timestep
-        for _ in range(args.warmup + args.steps):
+        n_e = 0
+        while (n_e < args.steps) if args.steps > 0 else (ts.time < pe.config.time_end):
             assert se.step(ts) == 0, se.error.message
+            n_e += 1
         se.sync_to_host(0)
         t1 = time.perf_counter()
         d2h = sum(pe.fields[f].nbytes for f in (abi.ELDENSITY, abi.ELENERGY, abi.ELPRESSURE,
@@ -296,12 +317,7 @@ def main():
                                                 abi.CNVISCX, abi.CNVISCY, abi.ELVISC, abi.ELMASS,
                                                 abi.CNMASS, abi.NDX, abi.NDY, abi.NDU, abi.NDV)
                   if f in pe.fields)
-        n_e = args.warmup + args.steps
-        e2e_val = nel * n_e / (t1 - t0)
-        if world > 1:
-            t = torch.tensor([t1 - t0], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_val = nel * n_e * world / float(t.item())
+        e2e_val, _, _ = job_rate((t1 - t0) * 1e3, nel * n_e, device="cuda")
         e2e = {"value": e2e_val, "unit": "zone-cycles/s",
                "h2d_bytes_per_step": int(h2d / n_e) + 2 * 64,
                "d2h_bytes_per_step": int(d2h / n_e) + 3 * 64,
@@ -313,8 +329,8 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu:
         rate, steps, t = cpu_baseline(deck, nel, target_s=12.0, cores=1)
         cpu = {"value": rate, "unit": "zone-cycles/s", "cores": 1, "kind": "port",
-               "sample": "%d steps of %s on one core (serial CPU restatement, "
-                         "-O2 -ffp-contract=off), %.1f s" % (steps, wname, t)}
+               "sample": "the first %d steps of %s from t=0 on one core (serial CPU "
+                         "restatement, -O2 -ffp-contract=off), %.1f s" % (steps, wname, t)}
 
     if rank == 0:
         line = {"metric": "zone-cycles/s FP64 (1 GB300, %HBM roof)", "value": value,
@@ -325,6 +341,7 @@ def main():
                 "config": {"workload": wname, "nel": nel, "fp_mode": args.fp,
                            "replicas": world, "l2": "working set %.0f MB > 129 MB L2, no flush"
                                                      % (step_bytes / 1e6),
+                           "timed": "%d steps from t=0 to t=%.4g" % (nsteps, t_end),
                            "loop": "bl_run device time loop, CUDA graphs of 16 steps"},
                 "roofline": roof, "fp64": fp64, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": launches, "clocks": clk.summary()}

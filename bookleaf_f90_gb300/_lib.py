@@ -48,6 +48,11 @@ def load(build_if_missing=True):
     L.bl_kernel_launches.argtypes = [vp]
     L.bl_kernel_launches.restype = ct.c_longlong
     L.bl_version.restype = ct.c_char_p
+    L.bl_selftest_fp64.argtypes = [ct.c_int, ct.c_longlong, ct.c_ulonglong, P(ct.c_longlong),
+                                   P(ct.c_double), P(ct.c_double)]
+    L.bl_selftest_fp64.restype = ct.c_int
+    L.bl_fp64_rates.argtypes = [P(ct.c_double), ct.c_int]
+    L.bl_fp64_rates.restype = ct.c_int
     L.bl_abi_sizes.argtypes = [P(ct.c_int), ct.c_int]
     L.bl_abi_sizes.restype = ct.c_int
     _lib = L
@@ -57,4 +62,17 @@ def load(build_if_missing=True):
 # Every exported entry point include/bookleaf_gb300.h declares.
 EXPORTS = ("bl_init", "bl_finalize", "bl_getdt", "bl_lagstep", "bl_alestep", "bl_run",
            "bl_sync_to_host", "bl_sync_to_device", "bl_synchronize", "bl_stream",
-           "bl_kernel_launches", "bl_version")
+           "bl_kernel_launches", "bl_version", "bl_getdt_noalloc", "bl_selftest_fp64",
+           "bl_fp64_rates")
+
+
+def fp64_rates():
+    """Measured issue rates on the current device, G operations/s: FP64
+    FMA, hardware and integer-pipe divide, hardware and integer-pipe square
+    root."""
+    L = load()
+    out = (ct.c_double * 5)()
+    if L.bl_fp64_rates(out, 5) != 0:
+        raise RuntimeError("bl_fp64_rates failed")
+    return {"dfma": out[0], "ddiv_hw": out[1], "ddiv_int": out[2], "dsqrt_hw": out[3],
+            "dsqrt_int": out[4]}

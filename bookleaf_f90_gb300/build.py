@@ -50,6 +50,7 @@ def build(force=False, verbose=False, extra=()):
         (common + ["-c", os.path.join(CSRC, "bl_capi.cu"), "-o", os.path.join(BUILD, "capi.o")]),
         (common + ["--fmad=true", "-c", os.path.join(CSRC, "bl_noalloc.cu"),
                    "-o", os.path.join(BUILD, "noalloc.o")]),
+        (common + ["-c", os.path.join(CSRC, "bl_selftest.cu"), "-o", os.path.join(BUILD, "selftest.o")]),
     ]
     procs = [subprocess.Popen(j, stdout=subprocess.PIPE, stderr=subprocess.STDOUT) for j in jobs]
     logs = []
@@ -64,7 +65,8 @@ def build(force=False, verbose=False, extra=()):
                                          os.path.join(BUILD, "k_fast.o"),
                                          os.path.join(BUILD, "k_exact.o"),
                                          os.path.join(BUILD, "capi.o"),
-                                         os.path.join(BUILD, "noalloc.o")])
+                                         os.path.join(BUILD, "noalloc.o"),
+                                         os.path.join(BUILD, "selftest.o")])
     os.replace(tmp, LIB)
     if verbose:
         sys.stdout.write("\n".join(logs))

@@ -70,9 +70,9 @@ __device__ __forceinline__ void elvl_pair(int iel, int i1, const int* nb, const 
   double w2 = elvar[iel1] - rv;
   double w3 = fabs(w1), w4 = fabs(w2);
   double w7 = copysign(1.0, w2);
-  double w8 = (w1 * w6 * w6 + w2 * w5 * w5) / (w5 * w6 * (w5 + w6));
-  double grad = w7 * minF(minF(fabs(w8), w3 / w5), w4 / w6);
-  if (w1 * w2 <= 0.0) grad = 0.0;
+  double w8 = DIV(w1 * w6 * w6 + w2 * w5 * w5, w5 * w6 * (w5 + w6));
+  double grad = w7 * minF(minF(fabs(w8), DIV(w3, w5)), DIV(w4, w6));
+  if (geF(0.0, w1 * w2)) grad = 0.0;
   o1 = r1 * (rv + grad * (r3 - 0.5 * r1));
   o2 = r2 * (rv - grad * (r4 - 0.5 * r2));
   (void)iel;
@@ -104,9 +104,9 @@ __global__ void __launch_bounds__(BS) k_ale_flux(DevFields F, DevCfg C) {
   for (int jj = 0; jj < 4; jj++) {
     const int jp = (jj + 1) & 3;
     double d = face_dv(x0[jj], x0[jp], y0[jj], y0[jp], x1[jp], x1[jj], y1[jp], y1[jj]);
-    fv[jj] = (d < zc) ? 0.0 : d;
+    fv[jj] = gtF(zc, d) ? 0.0 : d;
     double dn = -d;   // the neighbour's volume of the same face
-    fvn[jj] = (dn < zc) ? 0.0 : dn;
+    fvn[jj] = gtF(zc, dn) ? 0.0 : dn;
   }
   const int4 ee = __ldg(F.ielel + iel);
   const int nb[4] = {ee.x, ee.y, ee.z, ee.w};
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(BS) k_ale_el(DevFields F, DevCfg C) {
   F.mpr[iel] = mpr;
   F.vol[iel] = v1;
   F.mass[iel] = m1;
-  F.rho[iel] = m1 / v1;
+  F.rho[iel] = DIV(m1, v1);
   // ale_kn_fluxelvl(cnmass, fcdm, elenergy)
   const d4 cm = F.cnmass[iel];
   const double ob[4] = {cm.x, cm.y, cm.z, cm.w};
@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(BS) k_ale_el(DevFields F, DevCfg C) {
       const int ii = ilfcl + 2 * (icn - 1);
       const double cdb = cndm[ii];
       double rdu = 0.0, rdv = 0.0;
-      if (cdb > 0.0) {
+      if (gtF(cdb, 0.0)) {
         const int lnl = (ifcl + icn) % 4;
         const int lnr = (ifcl - icn + 1) % 4;
         const int4 m = __ldg(F.ielnd + iell);
@@ -239,14 +239,14 @@ __global__ void __launch_bounds__(BS) k_ale_el(DevFields F, DevCfg C) {
           double w2 = cvar[ilndr] - rv;
           double w3 = fabs(w1), w4 = fabs(w2);
           double w7 = copysign(1.0, w2);
-          double w8 = (w2 * w6 * w6 + w1 * w5 * w5) / den;
-          double grad = w7 * minF(minF(fabs(w8), w3 / w6), w4 / w5);
-          if (w1 * w2 <= 0.0) grad = 0.0;
+          double w8 = DIV(w2 * w6 * w6 + w1 * w5 * w5, den);
+          double grad = w7 * minF(minF(fabs(w8), DIV(w3, w6)), DIV(w4, w5));
+          if (geF(0.0, w1 * w2)) grad = 0.0;
           double rd = cdb * (rv + grad * rd0);
           if (q == 0) rdu = rd; else rdv = rd;
         }
       }
-      if (cdb < 0.0) {
+      if (gtF(0.0, cdb)) {
         const int lnl = (ifcr + icn - 2) % 4;
         const int lnr = (((ifcr - icn - 1) % 4) + 4) % 4;
         const int4 m = __ldg(F.ielnd + ielr);
@@ -264,9 +264,9 @@ __global__ void __launch_bounds__(BS) k_ale_el(DevFields F, DevCfg C) {
           double w2 = nvar[mm[lnr]] - rv;
           double w3 = fabs(w1), w4 = fabs(w2);
           double w7 = copysign(1.0, w2);
-          double w8 = (w1 * w6 * w6 + w2 * w5 * w5) / den;
-          double grad = -(w7 * minF(minF(fabs(w8), w3 / w5), w4 / w6));
-          if (w1 * w2 <= 0.0) grad = 0.0;
+          double w8 = DIV(w1 * w6 * w6 + w2 * w5 * w5, den);
+          double grad = -(w7 * minF(minF(fabs(w8), DIV(w3, w5)), DIV(w4, w6)));
+          if (geF(0.0, w1 * w2)) grad = 0.0;
           double rd = cdb * (rv + grad * rd0);
           if (q == 0) rdu = rd; else rdv = rd;
         }
@@ -315,8 +315,8 @@ __global__ void __launch_bounds__(BS) k_ale_nd(DevFields F, DevCfg C) {
   const bool au = (t != -1) && (t != -3);
   const bool av = (t != -2) && (t != -3);
   double u = F.ndu[ind], v = F.ndv[ind];
-  if (au && (m1 > cutm)) u = (u * m0 + fu) / m1;
-  if (av && (m1 > cutm)) v = (v * m0 + fv) / m1;
+  if (au && gtF(m1, cutm)) u = DIV(u * m0 + fu, m1);
+  if (av && gtF(m1, cutm)) v = DIV(v * m0 + fv, m1);
   F.ndu[ind] = u;
   F.ndv[ind] = v;
   // Eulerian vertex: x + dt*(-ubar)
@@ -352,7 +352,7 @@ __global__ void __launch_bounds__(BS) k_ale_update(DevFields F, DevCfg C) {
   const double m1 = F.mass[iel], mpr = F.mpr[iel];
   const double cut = F.vpr[iel] * C.dencut;
   double e = F.e[iel];
-  if (m1 > cut) e = (e * mpr + elf) / m1;
+  if (gtF(m1, cut)) e = DIV(e * mpr + elf, m1);
   // new corner masses (ale_kn_massbasisnd)
   const d4 cm = F.cnmass[iel], cf = F.cnflux[iel];
   F.cnmass[iel] = make_d4(cm.x + cf.x, cm.y + cf.y, cm.z + cf.z, cm.w + cf.w);
@@ -366,8 +366,8 @@ __global__ void __launch_bounds__(BS) k_ale_update(DevFields F, DevCfg C) {
     y[j] = F.ndy[n[j]];
   }
   Iso g = getiso(x, y);
-  if (g.vol < 0.0) atomicMax(&F.step->negvol_ale, iel + 1);
-  const double rho = m1 / g.vol;
+  if (gtF(0.0, g.vol)) atomicMax(&F.step->negvol_ale, iel + 1);
+  const double rho = DIV(m1, g.vol);
   double p, cs2;
   eos_pc(C, __ldg(F.ielmat + iel), rho, e, p, cs2);
   F.a1[iel] = g.a1;
@@ -390,7 +390,7 @@ __global__ void __launch_bounds__(BS) k_ale_update(DevFields F, DevCfg C) {
     for (int k = 0; k < nc; k++) {
       const int icp = c0 + k;
       const double cpv = 4.0 * (g.a1 * g.b3 - g.a3 * g.b1) * F.frvol[icp];
-      const double cpr = F.cpm[icp] / cpv;
+      const double cpr = DIV(F.cpm[icp], cpv);
       double cpp, cpc;
       eos_pc(C, __ldg(F.icpmat + icp), cpr, F.cpe[icp], cpp, cpc);
       F.cpvol[icp] = cpv;

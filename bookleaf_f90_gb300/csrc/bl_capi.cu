@@ -39,6 +39,8 @@ struct bl_ctx {
   cudaGraphExec_t gexec = nullptr;
   int gsteps = 0;
   bool g_ale = false;
+  bl::StepRec* g_hist = nullptr;  // history buffer and record limit the
+  int g_maxrec = -1;              // graph's kernel arguments were captured with
   int hist_cap = 0;
   std::vector<int> ielmat_h;  // for timestep%mdt
 };
@@ -131,6 +133,7 @@ void header_from_ts(bl_ctx* x, const bl_timestep* ts, int run_mode) {
   h.time = ts->time;
   h.dt = ts->dt;
   h.dts = ts->dts;
+  h.rdt = 1.0 / ts->dt;  // IEEE division: the device's DIV(1.0, dt) bit for bit
   h.nstep = ts->nstep;
   h.idtel = ts->idtel;
   h.run_mode = run_mode;
@@ -660,28 +663,27 @@ int bl_run(bl_ctx* x, bl_timestep* ts, int max_steps, bl_step_record* history, i
     r = cudaMalloc(&x->F.hist, sizeof(bl::StepRec) * (size_t)max_steps);
     if (r != cudaSuccess) return cuda_fail(e, r, "bl_run");
     x->hist_cap = max_steps;
-    if (x->gexec) {  // captured with the old history pointer
-      cudaGraphExecDestroy(x->gexec);
-      x->gexec = nullptr;
-    }
   }
-  x->C.max_records = history ? x->hist_cap : 0;
-  bl::StepRec* keep_hist = x->F.hist;
-  if (!history) x->F.hist = nullptr;
+  // the kernels of this run see the history buffer only when one is wanted
+  bl::DevFields F = x->F;
+  bl::DevCfg C = x->C;
+  if (!history) F.hist = nullptr;
+  C.max_records = history ? x->hist_cap : 0;
   const bool with_ale = x->c.ale_zexist != 0;
   const int G = 16;  // steps per graph launch
-  if (!x->gexec || x->gsteps != G || x->g_ale != with_ale || (!history) != (x->C.max_records == 0)) {
+  if (!x->gexec || x->gsteps != G || x->g_ale != with_ale || x->g_hist != F.hist ||
+      x->g_maxrec != C.max_records) {
     if (x->gexec) cudaGraphExecDestroy(x->gexec);
     x->gexec = nullptr;
     cudaGraph_t g;
     r = cudaStreamBeginCapture(x->stream, cudaStreamCaptureModeThreadLocal);
     if (r != cudaSuccess) return cuda_fail(e, r, "bl_run capture");
     for (int k = 0; k < G; k++) {
-      x->L.getdt(x->F, x->C, x->stream);
-      x->L.lag_force(x->F, x->C, x->stream);
-      x->L.lag_accel(x->F, x->C, x->stream);
-      x->L.lag_state(x->F, x->C, x->stream);
-      if (with_ale) x->L.ale(x->F, x->C, x->stream);
+      x->L.getdt(F, C, x->stream);
+      x->L.lag_force(F, C, x->stream);
+      x->L.lag_accel(F, C, x->stream);
+      x->L.lag_state(F, C, x->stream);
+      if (with_ale) x->L.ale(F, C, x->stream);
     }
     r = cudaStreamEndCapture(x->stream, &g);
     if (r != cudaSuccess) return cuda_fail(e, r, "bl_run capture");
@@ -690,6 +692,8 @@ int bl_run(bl_ctx* x, bl_timestep* ts, int max_steps, bl_step_record* history, i
     if (r != cudaSuccess) return cuda_fail(e, r, "bl_run instantiate");
     x->gsteps = G;
     x->g_ale = with_ale;
+    x->g_hist = F.hist;
+    x->g_maxrec = C.max_records;
   }
   header_from_ts(x, ts, 1);
   // step limit: getdt stops once nrecord reaches it (DevStep.nrecord counts)
@@ -706,11 +710,11 @@ int bl_run(bl_ctx* x, bl_timestep* ts, int max_steps, bl_step_record* history, i
       launched += G;
     } else {
       for (int k = 0; k < remaining; k++) {
-        x->L.getdt(x->F, x->C, x->stream);
-        x->L.lag_force(x->F, x->C, x->stream);
-        x->L.lag_accel(x->F, x->C, x->stream);
-        x->L.lag_state(x->F, x->C, x->stream);
-        if (with_ale) x->L.ale(x->F, x->C, x->stream);
+        x->L.getdt(F, C, x->stream);
+        x->L.lag_force(F, C, x->stream);
+        x->L.lag_accel(F, C, x->stream);
+        x->L.lag_state(F, C, x->stream);
+        if (with_ale) x->L.ale(F, C, x->stream);
       }
       x->launches += (long long)remaining * per_step;
       launched += remaining;
@@ -728,7 +732,8 @@ int bl_run(bl_ctx* x, bl_timestep* ts, int max_steps, bl_step_record* history, i
   if (nsteps) *nsteps = nrec;
   if (history && nrec > 0) {
     std::vector<bl::StepRec> tmp(nrec);
-    cudaMemcpy(tmp.data(), x->F.hist, sizeof(bl::StepRec) * nrec, cudaMemcpyDeviceToHost);
+    r = cudaMemcpy(tmp.data(), F.hist, sizeof(bl::StepRec) * nrec, cudaMemcpyDeviceToHost);
+    if (r != cudaSuccess) return cuda_fail(e, r, "bl_run history");
     for (int i = 0; i < nrec; i++) {
       history[i].time = tmp[i].time;
       history[i].dt = tmp[i].dt;
@@ -738,7 +743,6 @@ int bl_run(bl_ctx* x, bl_timestep* ts, int max_steps, bl_step_record* history, i
       history[i].ierr = tmp[i].ierr;
     }
   }
-  x->F.hist = keep_hist;
   x->cs2_is_v = false;
   fill_ts_from_step(x, S, ts);
   ts->zcorrector = 1;

@@ -14,6 +14,7 @@
 //                   reference's scatter loops, so node sums are computed by
 //                   gathers without atomics and are deterministic.
 #pragma once
+#include "bl_fp64.cuh"
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -29,6 +30,7 @@ __host__ __device__ __forceinline__ d4 make_d4(double x, double y, double z, dou
 // it back once per bl_getdt call; bl_run never reads it inside the loop.
 struct DevStep {
   double time, dt, dts;
+  double rdt;           // 1/dt (hourglass filter), set with dt
   double cfl_rdt, div_rdt;
   int nstep, idtel, sdt, imdt;
   int cfl_idt, div_idt;
@@ -114,10 +116,15 @@ struct DevFields {
 
 // ---------------------------------------------------------------- helpers
 
-// Fortran MAX/MIN as the CPU restatement evaluates them: the first argument
-// is returned on ties.
-__device__ __forceinline__ double maxF(double a, double b) { return (b > a) ? b : a; }
-__device__ __forceinline__ double minF(double a, double b) { return (b < a) ? b : a; }
+// Fortran MAX/MIN as the CPU restatement evaluates them, (b > a) ? b : a
+// and (b < a) ? b : a: the first argument is returned on ties and when
+// either is NaN.  The comparison runs on the integer pipe (bl_fp64.cuh).
+__device__ __forceinline__ double maxF(double a, double b) { return gtF(b, a) ? b : a; }
+__device__ __forceinline__ double minF(double a, double b) { return gtF(a, b) ? b : a; }
+// the same, cheaper, when the sign bit is known to be clear (a square root,
+// an absolute value, a sum of squares): of a for maxF_nn, of b for minF_nn
+__device__ __forceinline__ double maxF_nn(double a, double b) { return gt_nn(b, a) ? b : a; }
+__device__ __forceinline__ double minF_nn(double a, double b) { return gt_nn(a, b) ? b : a; }
 // Fortran SIGN(a,b): |a| with the sign bit of b (negative zero honoured).
 __device__ __forceinline__ double signF(double a, double b) { return copysign(fabs(a), b); }
 

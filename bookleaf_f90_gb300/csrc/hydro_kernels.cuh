@@ -28,7 +28,18 @@
 #include <cmath>
 
 #include "bl_device.cuh"
+#include "bl_fp64.cuh"
 #include "bl_kernels.h"
+
+// Every FP64 division and square root of the path goes through the
+// integer-pipe versions, which return the IEEE results bit for bit
+// (bl_fp64.cuh).
+#ifndef DIV
+#define DIV(a, b) ::bl::ddiv_rn((a), (b))
+#endif
+#ifndef SQRT
+#define SQRT(a) ::bl::dsqrt_rn(a)
+#endif
 
 namespace bl {
 namespace BL_NS {
@@ -47,34 +58,34 @@ __device__ __forceinline__ void eos_pc(const DevCfg& C, int mat, double rho, dou
     p = __ldg(P);
     cs2 = C.ccut;
   } else if (t == 2) {
-    double t1 = rho / __ldg(P + 2);
+    double t1 = DIV(rho, __ldg(P + 2));
     p = __ldg(P) * (pow(t1, __ldg(P + 1)) - 1.0);
     p = maxF(p, __ldg(P + 3));
     double t2 = __ldg(P + 1) - 1.0;
-    cs2 = (__ldg(P) * __ldg(P + 1)) / __ldg(P + 2);
+    cs2 = DIV(__ldg(P) * __ldg(P + 1), __ldg(P + 2));
     cs2 = cs2 * pow(t1, t2);
   } else if (t == 3) {
-    double t1 = __ldg(P + 3) * __ldg(P + 5) / rho;
-    double t2 = __ldg(P + 4) * __ldg(P + 5) / rho;
+    double t1 = DIV(__ldg(P + 3) * __ldg(P + 5), rho);
+    double t2 = DIV(__ldg(P + 4) * __ldg(P + 5), rho);
     double t3 = __ldg(P) * rho * e;
-    double t4 = (1.0 - __ldg(P) / t1) * __ldg(P + 1) * exp(-t1);
-    double t5 = (1.0 - __ldg(P) / t2) * __ldg(P + 2) * exp(-t2);
+    double t4 = (1.0 - DIV(__ldg(P), t1)) * __ldg(P + 1) * exp(-t1);
+    double t5 = (1.0 - DIV(__ldg(P), t2)) * __ldg(P + 2) * exp(-t2);
     p = t3 + t4 + t5;
     double pp = p;
-    if (fabs(pp) < C.pcut) pp = 0.0;
-    double q1 = __ldg(P + 5) / rho;
+    if (gt_nn(C.pcut, fabs(pp))) pp = 0.0;
+    double q1 = DIV(__ldg(P + 5), rho);
     double s3 = __ldg(P + 3) * q1;
-    double u4 = __ldg(P) / __ldg(P + 3) + __ldg(P) * q1 - s3 * q1;
+    double u4 = DIV(__ldg(P), __ldg(P + 3)) + __ldg(P) * q1 - s3 * q1;
     u4 = u4 * __ldg(P + 1) * exp(-s3);
     s3 = __ldg(P + 4) * q1;
-    double u5 = __ldg(P) / __ldg(P + 4) + __ldg(P) * q1 - s3 * q1;
+    double u5 = DIV(__ldg(P), __ldg(P + 4)) + __ldg(P) * q1 - s3 * q1;
     u5 = u5 * __ldg(P + 2) * exp(-s3);
-    cs2 = __ldg(P) * pp / rho + __ldg(P) * e - u4 - u5;
+    cs2 = DIV(__ldg(P) * pp, rho) + __ldg(P) * e - u4 - u5;
   } else {
     p = -1.0;
     cs2 = C.ccut;
   }
-  if (fabs(p) < C.pcut) p = 0.0;
+  if (gt_nn(C.pcut, fabs(p))) p = 0.0;
   cs2 = maxF(cs2, C.ccut);
 }
 
@@ -131,13 +142,13 @@ __device__ __forceinline__ double min_dln(const double* x, const double* y, doub
     // k,k+1 midpoint... in the reference's argument order
     const int a = k, b = (k + 1) & 3, c = (k + 2) & 3, d = (k + 3) & 3;
     double w1 = g_denom(x[c], y[c], x[d], y[d]);
-    if (w1 < zcut) r[k] = g_distpp(x[a], y[a], x[b], y[b], x[c], y[c]);
-    else r[k] = g_distpl(x[a], y[a], x[b], y[b], x[c], y[c], x[d], y[d]) / w1;
+    if (gt_nn(zcut, w1)) r[k] = g_distpp(x[a], y[a], x[b], y[b], x[c], y[c]);
+    else r[k] = DIV(g_distpl(x[a], y[a], x[b], y[b], x[c], y[c], x[d], y[d]), w1);
   }
-  double m = r[0];
-  m = minF(m, r[1]);
-  m = minF(m, r[2]);
-  m = minF(m, r[3]);
+  double m = r[0];  // all four are sums of squares or their quotients
+  m = minF_nn(m, r[1]);
+  m = minF_nn(m, r[2]);
+  m = minF_nn(m, r[3]);
   return m;
 }
 
@@ -155,9 +166,9 @@ __device__ __forceinline__ double min_dlm(const double* x, const double* y) {
   y1 = 0.5 * (y1 - y2);
   double r1 = x1 * x1 + y1 * y1;
   double m = r0;
-  m = minF(m, r1);
-  m = minF(m, r0);
-  m = minF(m, r1);
+  m = minF_nn(m, r1);
+  m = minF_nn(m, r0);
+  m = minF_nn(m, r1);
   return m;
 }
 
@@ -202,7 +213,7 @@ __device__ void force_sp(double w1, double rho, double cs2, const double* cx, co
     double w5 = 0.25 * (-y1 + y2 + y3 - y4);
     double w6 = 0.25 * (-y1 - y2 + y3 + y4);
     double w2 = 4.0 * (w3 * w6 - w4 * w5);
-    w2 = c4(spm, j1) / w2;
+    w2 = DIV(c4(spm, j1), w2);
     w2 = w2 - rho;
     w2 = cs2 * w2;
     lfx[j1][0] = w2 * (w5 - w6);
@@ -259,7 +270,7 @@ __device__ __forceinline__ double energy_update(double e, double m, double zeroc
                                                 const double* u, const double* v) {
   double w1 = fx[0] * u[0] + fy[0] * v[0] + fx[1] * u[1] + fy[1] * v[1] + fx[2] * u[2] +
               fy[2] * v[2] + fx[3] * u[3] + fy[3] * v[3];
-  w1 = -(w1 / maxF(m, zerocut));
+  w1 = -DIV(w1, maxF(m, zerocut));
   return e + w1 * dt;
 }
 
@@ -273,14 +284,19 @@ __device__ __forceinline__ bool halted(const DevStep* S) {
 // on ties (hydro_kn_getdt.f90:70-73).  DIV: largest value above TINY, first
 // index on ties, (TINY,-1) when no element exceeds TINY (:103-116).
 __device__ __forceinline__ void cfl_min(double& v, int& i, double ov, int oi) {
-  if (ov < v || (ov == v && oi < i)) { v = ov; i = oi; }
+  const long long ko = okey(ov), kv = okey(v);
+  const bool ord = !nanF(ov) && !nanF(v);
+  if (ord && (ko < kv || (ko == kv && oi < i))) { v = ov; i = oi; }
 }
+// DIV candidates are TINY or values that exceeded it: positive, never NaN,
+// so their bit patterns order as integers
 __device__ __forceinline__ void div_max(double& v, int& i, double ov, int oi) {
-  if (ov > v || (ov == v && oi >= 0 && (i < 0 || oi < i))) { v = ov; i = oi; }
+  const long long io = __double_as_longlong(ov), iv = __double_as_longlong(v);
+  if (io > iv || (io == iv && oi >= 0 && (i < 0 || oi < i))) { v = ov; i = oi; }
 }
 
 template <int BS>
-__global__ void __launch_bounds__(BS) k_getdt(DevFields F, DevCfg C) {
+__global__ void __launch_bounds__(BS, 4) k_getdt(DevFields F, DevCfg C) {
   DevStep* S = F.step;
   if (halted(S)) return;
   if (S->stop_next) {            // bl_run: the previous step reached time_end
@@ -334,21 +350,21 @@ __global__ void __launch_bounds__(BS) k_getdt(DevFields F, DevCfg C) {
         for (int e2 = 0; e2 < 2; e2++) {
           const int is = e2 == 0 ? ((s + 3) & 3) : (s + 1);
           double w1 = du[is], w2 = dv[is], w3 = dx[is], w4 = dy[is];
-          double den = sqrt(w1 * w1 + w2 * w2);
+          double den = SQRT(w1 * w1 + w2 * w2);
           lu[is] = den;
-          den = 1.0 / maxF(den, zc);
+          den = DIV(1.0, maxF_nn(den, zc));
           double uhat = w1 * den, vhat = w2 * den;
-          den = sqrt(w3 * w3 + w4 * w4);
+          den = SQRT(w3 * w3 + w4 * w4);
           lx[is] = den;
-          den = 1.0 / maxF(den, zc);
+          den = DIV(1.0, maxF_nn(den, zc));
           double xhat = w3 * den, yhat = w4 * den;
           uh[is] = uhat;
           vh[is] = vhat;
           xh[is] = xhat;
           yh[is] = yhat;
           den = w3 * xhat + w4 * yhat;
-          w1 = (w1 * uhat + w2 * vhat) / signF(maxF(fabs(den), zc), den);
-          w1 = 1.0 / signF(maxF(fabs(w1), zc), w1);
+          w1 = DIV(w1 * uhat + w2 * vhat, signF(maxF_nn(fabs(den), zc), den));
+          w1 = DIV(1.0, signF(maxF_nn(fabs(w1), zc), w1));
           // neighbour faces: edge 1 uses MOD(ielfc,4)+1 / MOD(ielfc+2,4)+1,
           // edge 2 the other pair (hydro_kn_edgeviscosity.f90:117-151)
           const int ins1 = e2 == 0 ? ((f1 + 1) & 3) : ((f1 + 3) & 3);
@@ -361,7 +377,7 @@ __global__ void __launch_bounds__(BS) k_getdt(DevFields F, DevCfg C) {
             double ddx = F.ndx[b] - F.ndx[a], ddy = F.ndy[b] - F.ndy[a];
             double ddu = F.ndu[b] - F.ndu[a], ddv = F.ndv[b] - F.ndv[a];
             double dn = ddx * xhat + ddy * yhat;
-            double q = (ddu * uhat + ddv * vhat) / signF(maxF(fabs(dn), zc), dn);
+            double q = DIV(ddu * uhat + ddv * vhat, signF(maxF_nn(fabs(dn), zc), dn));
             r1 = q * w1;
           }
           if (in2 != iel) {
@@ -371,7 +387,7 @@ __global__ void __launch_bounds__(BS) k_getdt(DevFields F, DevCfg C) {
             double ddx = F.ndx[b] - F.ndx[a], ddy = F.ndy[b] - F.ndy[a];
             double ddu = F.ndu[b] - F.ndu[a], ddv = F.ndv[b] - F.ndv[a];
             double dn = ddx * xhat + ddy * yhat;
-            double q = (ddu * uhat + ddv * vhat) / signF(maxF(fabs(dn), zc), dn);
+            double q = DIV(ddu * uhat + ddv * vhat, signF(maxF_nn(fabs(dn), zc), dn));
             r2 = q * w1;
           }
           sc[is][0] = r1;
@@ -397,15 +413,15 @@ __global__ void __launch_bounds__(BS) k_getdt(DevFields F, DevCfg C) {
         for (int e2 = 0; e2 < 2; e2++) {
           const int is = e2 == 0 ? is1 : is2;
           const int ins = nb[is];
-          double w1 = C.cvisc1 * sqrt(0.5 * (cs2i + F.cs2[ins]));
+          double w1 = C.cvisc1 * SQRT(0.5 * (cs2i + F.cs2[ins]));
           double w2 = sc[is][0], w3 = sc[is][1];
           w2 = minF(minF(minF(0.5 * (w2 + w3), 2.0 * w2), 2.0 * w3), 1.0);
           w2 = maxF(0.0, w2);
           double w4 = lu[is];
           w3 = 0.5 * (1.0 - w2) * (rho0 + F.rho[ins]) * (w1 + C.cvisc2 * w4);
           edv[is] = w3;
-          w4 = 2.0 * w4 / maxF(rho0, zc);
-          visc = maxF(visc, w3 * w4);
+          w4 = DIV(2.0 * w4, maxF(rho0, zc));
+          visc = maxF_nn(visc, w3 * w4);  // visc stays +0 or positive
         }
       }
       // hydro_kn_geteviscosity (hydro_kn_edgeviscosity.f90:219-282)
@@ -417,9 +433,9 @@ __global__ void __launch_bounds__(BS) k_getdt(DevFields F, DevCfg C) {
         const int ins = (f + 1) & 3;
         double w3 = 0.5 * (x[f] + x[ins]);
         double w6 = 0.5 * (y[f] + y[ins]);
-        double w7 = sqrt((xc - w3) * (xc - w3) + (yc - w6) * (yc - w6));
+        double w7 = SQRT((xc - w3) * (xc - w3) + (yc - w6) * (yc - w6));
         double w8 = lx[f];  // SQRT(w1*w1+w4*w4) of the same face difference
-        double den = 1.0 / w7;
+        double den = DIV(1.0, w7);
         double xhat = (yc - w6) * den, yhat = (w3 - xc) * den;
         // w1*(1/w8), w4*(1/w8): equal to the limiter's normalised face
         // vector whenever w8 > zerocut; otherwise the edge is cut below
@@ -431,10 +447,10 @@ __global__ void __launch_bounds__(BS) k_getdt(DevFields F, DevCfg C) {
         double uhat = du[f], vhat = dv[f];
         double w5 = lu[f];
         double w6b = uhat * xhat + vhat * yhat;
-        den = w6b / maxF(w5, zc);
+        den = DIV(w6b, maxF_nn(w5, zc));
         edx[f] = edv[f] * uhat * den;
         edy[f] = edv[f] * vhat * den;
-        if ((w5 <= zc) || (w6b <= zc) || (w7 <= zc) || (w8 <= zc)) {
+        if (le_nn(w5, zc) || geF(zc, w6b) || le_nn(w7, zc) || le_nn(w8, zc)) {
           edx[f] = 0.0;
           edy[f] = 0.0;
         }
@@ -470,7 +486,7 @@ __global__ void __launch_bounds__(BS) k_getdt(DevFields F, DevCfg C) {
       r11 = DBL_MAX;
     } else {
       double w1 = __ldg(C.zmidlength + ireg) ? min_dlm(x, y) : min_dln(x, y, C.zcut);
-      r11 = w1 / cs2v;
+      r11 = DIV(w1, cs2v);
     }
     cflv = r11;
     cfli = iel;
@@ -478,8 +494,8 @@ __global__ void __launch_bounds__(BS) k_getdt(DevFields F, DevCfg C) {
     const double A1 = F.a1[iel], A3 = F.a3[iel], B1 = F.b1[iel], B3 = F.b3[iel];
     double w1 = u[0] * (-B3 + B1) + v[0] * (A3 - A1) + u[1] * (B3 + B1) + v[1] * (-A3 - A1) +
                 u[2] * (B3 - B1) + v[2] * (-A3 + A1) + u[3] * (-B3 - B1) + v[3] * (A3 + A1);
-    w1 = fabs(w1) / F.vol[iel];
-    if (w1 > divv) {
+    w1 = DIV(fabs(w1), F.vol[iel]);
+    if (gt_nn(w1, divv)) {  // divv is TINY or a larger positive value
       divv = w1;
       divi = iel;
     }
@@ -561,8 +577,8 @@ __global__ void __launch_bounds__(BS) k_getdt(DevFields F, DevCfg C) {
     if (S->run_mode) S->halted = 1;
     return;
   }
-  const double rdt_cfl = C.cfl_sf * sqrt(cflv);
-  const double rdt_div = C.div_sf / divv;
+  const double rdt_cfl = C.cfl_sf * SQRT(cflv);
+  const double rdt_div = DIV(C.div_sf, divv);
   S->cfl_rdt = rdt_cfl;
   S->cfl_idt = cfli + 1;
   S->div_rdt = rdt_div;
@@ -576,6 +592,7 @@ __global__ void __launch_bounds__(BS) k_getdt(DevFields F, DevCfg C) {
   if (rdt_div < mind) { mind = rdt_div; mini = divi + 1; mins = 4; }
   S->nstep = S->nstep + 1;
   S->dt = mind;
+  S->rdt = DIV(1.0, mind);
   S->sdt = mins;
   S->idtel = mini;
   S->time = S->time + mind;
@@ -603,7 +620,7 @@ __global__ void __launch_bounds__(BS) k_getdt(DevFields F, DevCfg C) {
 // ================================================================ k_lag_force
 
 template <int BS>
-__global__ void __launch_bounds__(BS) k_lag_force(DevFields F, DevCfg C) {
+__global__ void __launch_bounds__(BS, 4) k_lag_force(DevFields F, DevCfg C) {
   const DevStep* S = F.step;
   if (halted(S)) return;
   const int iel = blockIdx.x * BS + threadIdx.x;
@@ -641,8 +658,8 @@ __global__ void __launch_bounds__(BS) k_lag_force(DevFields F, DevCfg C) {
   }
   // ---- geometry, density (geometry_dr_getgeometry, density_dr_getdensity)
   Iso g = getiso(xh, yh);
-  if (g.vol < 0.0) atomicMax(&F.step->negvol_pred, iel + 1);
-  const double rho = m / g.vol;
+  if (gtF(0.0, g.vol)) atomicMax(&F.step->negvol_pred, iel + 1);
+  const double rho = DIV(m, g.vol);
   // ---- energy (hydro_kn_getenergy with dts = dt/2) and EoS
   const double eh = energy_update(e0, m, zc, hdt, fx, fy, u, v);
   double ph, cs2h;
@@ -669,7 +686,7 @@ __global__ void __launch_bounds__(BS) k_lag_force(DevFields F, DevCfg C) {
       const double cpe = energy_update(F.cpe[icp], cpm, zc, hdt, cfx, cfy, cu, cv);
       F.cpe[icp] = cpe;  // the reference does not restore component energy
       const double cpv = 4.0 * (g.a1 * g.b3 - g.a3 * g.b1) * fr;
-      const double cpr = cpm / cpv;
+      const double cpr = DIV(cpm, cpv);
       double cpp, cpc;
       eos_pc(C, __ldg(F.icpmat + icp), cpr, cpe, cpp, cpc);
       // corrector component force at the half-step state
@@ -693,7 +710,7 @@ __global__ void __launch_bounds__(BS) k_lag_force(DevFields F, DevCfg C) {
     force_pq(ph, g.a1, g.a3, g.b1, g.b3, qx, qy, fx, fy);
     if (C.zsp)
       force_sp(__ldg(C.pmeritreg + ireg), rho, cs2h, xh, yh, F.spmass[iel], fx, fy);
-    if (C.zhg) force_hg(__ldg(C.kappareg + ireg), rho, g.vol, 1.0 / dt, u, v, fx, fy);
+    if (C.zhg) force_hg(__ldg(C.kappareg + ireg), rho, g.vol, S->rdt, u, v, fx, fy);
   }
   F.cnfx[iel] = make_d4(fx[0], fx[1], fx[2], fx[3]);
   F.cnfy[iel] = make_d4(fy[0], fy[1], fy[2], fy[3]);
@@ -720,11 +737,11 @@ __global__ void __launch_bounds__(BS) k_lag_accel(DevFields F, DevCfg C) {
     const double* cm = reinterpret_cast<const double*>(F.cnmass + iel);
     const double cmj = cm[jj];
     const double cw = reinterpret_cast<const double*>(F.cnwt_h + iel)[jj];
-    if (cmj > zc) {
+    if (gtF(cmj, zc)) {
       ndm = ndm + cmj;
     } else {
       const double cmi = cm[(jj + 3) & 3];
-      if (cmi > zc) ndm = ndm + cmi;
+      if (gtF(cmi, zc)) ndm = ndm + cmi;
       else ndm = ndm + F.rho_h[iel] * cw;
     }
     nda = nda + cw;
@@ -734,9 +751,9 @@ __global__ void __launch_bounds__(BS) k_lag_accel(DevFields F, DevCfg C) {
   // hydro_kn_getacceleration
   const double w1 = C.dencut * nda;
   double ax, ay;
-  if (ndm > w1) {
-    ax = fx / ndm;
-    ay = fy / ndm;
+  if (gtF(ndm, w1)) {
+    ax = DIV(fx, ndm);
+    ay = DIV(fy, ndm);
   } else {
     ax = 0.0;
     ay = 0.0;
@@ -747,7 +764,7 @@ __global__ void __launch_bounds__(BS) k_lag_accel(DevFields F, DevCfg C) {
   else if (t == -2) ay = 0.0;
   else if (t == -3) { ax = 0.0; ay = 0.0; }
   const double w2 = ax * ax + ay * ay;
-  if (w2 < C.accut * C.accut) {
+  if (gt_nn(C.accut * C.accut, w2)) {  // w2 is a sum of squares
     ax = 0.0;
     ay = 0.0;
   }
@@ -790,9 +807,9 @@ __global__ void __launch_bounds__(BS) k_lag_state(DevFields F, DevCfg C) {
     vb[j] = F.ndvbar[n[j]];
   }
   Iso g = getiso(x, y);
-  if (g.vol < 0.0) atomicMax(&F.step->negvol_corr, iel + 1);
+  if (gtF(0.0, g.vol)) atomicMax(&F.step->negvol_corr, iel + 1);
   const double m = F.mass[iel];
-  const double rho = m / g.vol;
+  const double rho = DIV(m, g.vol);
   const d4 f4x = F.cnfx[iel], f4y = F.cnfy[iel];
   const double fx[4] = {f4x.x, f4x.y, f4x.z, f4x.w};
   const double fy[4] = {f4y.x, f4y.y, f4y.z, f4y.w};
@@ -828,7 +845,7 @@ __global__ void __launch_bounds__(BS) k_lag_state(DevFields F, DevCfg C) {
       const double cpm = F.cpm[icp];
       const double cpe = energy_update(F.cpe[icp], cpm, zc, dt, cfx, cfy, cu, cv);
       const double cpv = 4.0 * (g.a1 * g.b3 - g.a3 * g.b1) * fr;
-      const double cpr = cpm / cpv;
+      const double cpr = DIV(cpm, cpv);
       double cpp, cpc;
       eos_pc(C, __ldg(F.icpmat + icp), cpr, cpe, cpp, cpc);
       F.cpe[icp] = cpe;

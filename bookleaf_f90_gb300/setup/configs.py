@@ -84,8 +84,13 @@ def sod_reference(nx=100, ny=10, time_end=20.0, eulerian=False):
     return sod(nx, ny, time_end=time_end, eulerian=eulerian, scale=100.0)
 
 
-def sedov(n=512, time_end=1.0, eulerian=False, gamma=1.4, energy=0.244816):
+def sedov(n=512, time_end=1.0, eulerian=False, gamma=1.4, energy=0.244816, kappa=None):
+    """Sedov blast on the quarter domain [0,1.2]^2.  ``kappa`` adds the
+    hourglass filter (kappaall) that the reference's own Sedov decks set
+    (input/sedov_lag_small: 0.01); without it the Lagrangian mesh tangles at
+    the origin long before t = 1 and the run stops on dt < dt_min."""
     ale = "&ALE\n zeul=.TRUE.\n/\n" if eulerian else ""
+    hg = "" if kappa is None else f" kappaall={kappa!r}\n"
     return f"""&CONTROL
  time_start=0.0
  time_end={time_end!r}
@@ -96,7 +101,7 @@ def sedov(n=512, time_end=1.0, eulerian=False, gamma=1.4, energy=0.244816):
  cfl_sf=0.5
  cvisc1=0.5
  cvisc2=0.75
-/
+{hg}/
 &EOS
  eos_type(1)='ideal gas'
  eos_param(1,1)={gamma!r}

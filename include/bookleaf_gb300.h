@@ -211,6 +211,22 @@ long long bl_kernel_launches(bl_ctx *ctx);
 /* Library version string. */
 const char *bl_version(void);
 
+/* Self-test of the integer-pipe FP64 arithmetic the kernels use in place of
+ * the hardware divide and square root (no counterpart in the reference): n
+ * operands (random, plus hard cases) are computed both ways on the current
+ * device; *mismatches receives the number of results that differ in any
+ * bit, first_a/first_b the first failing operands.  op 0: division a/b;
+ * op 1: square root of a.  Returns 0, or -1 when CUDA fails. */
+int bl_selftest_fp64(int op, long long n, unsigned long long seed, long long *mismatches,
+                     double *first_a, double *first_b);
+
+/* Issue rates on the current device, in G operations/s (no counterpart in
+ * the reference): rates[0] FP64 FMA, [1] hardware divide, [2] integer-pipe
+ * divide, [3] hardware square root, [4] integer-pipe square root.  n >= 5.
+ * The FMA rate is the FP64 roof the hot path's kernels are measured
+ * against.  Returns 0, or -1 when CUDA fails. */
+int bl_fp64_rates(double *rates, int n);
+
 /* ---- allocation-free getdt ---------------------------------------------- */
 
 /* Largest mesh bl_getdt_noalloc accepts: its reduction scratch lives in a

@@ -81,6 +81,75 @@ def test_device_loop_matches_per_call():
     assert not compare(pb, pa, exact=True)
 
 
+def test_device_loop_history_toggle():
+    """Runs with and without a history buffer in turn: each run's records are
+    its own steps, and the state matches the per-call path."""
+    base = Problem.from_deck(configs.sedov(16, time_end=1.0))
+    pa, pb = base.copy(), base.copy()
+    sa = Solver(pa, fp_mode=abi.FP_EXACT)
+    ierr, h1 = sa.run(max_steps=20)
+    assert ierr == 0 and [r[0] for r in h1] == list(range(1, 21))
+    ierr, h2 = sa.run(max_steps=20, history=False)
+    assert ierr == 0 and h2 == []
+    ierr, h3 = sa.run(max_steps=20)
+    assert ierr == 0 and [r[0] for r in h3] == list(range(41, 61))
+    sb = Solver(pb, fp_mode=abi.FP_EXACT)
+    times = []
+    for _ in range(60):
+        assert sb.step() == 0
+        times.append(pb.timestep.time)
+    assert [r[1] for r in h1] == times[:20]
+    assert [r[1] for r in h3] == times[40:]
+    sa.sync_to_host(0)
+    sb.sync_to_host(0)
+    assert not compare(pa, pb, exact=True)
+
+
+def test_restart_from_host_state():
+    """bl_sync_to_device replaces the whole device state: a context that ran
+    a few steps and is then given its initial fields again runs exactly as a
+    fresh one (the benchmark's warm-up relies on this)."""
+    base = Problem.from_deck(configs.sedov(16, kappa=0.01))
+    pa, pb = base.copy(), base.copy()
+    sa = Solver(pa, fp_mode=abi.FP_EXACT)
+    init = {fid: a.copy() for fid, a in pa.fields.items()}
+    ts0 = pa.timestep.copy()
+    ierr, _ = sa.run(max_steps=5, ts=pa.timestep.copy(), history=False)
+    assert ierr == 0
+    for fid, a in init.items():
+        np.copyto(pa.fields[fid], a)
+    sa.sync_to_device(0)
+    ta = ts0.copy()
+    ierr, _ = sa.run(max_steps=30, ts=ta, history=False)
+    assert ierr == 0, sa.error.message
+    sb = Solver(pb, fp_mode=abi.FP_EXACT)
+    tb = pb.timestep
+    ierr, _ = sb.run(max_steps=30, ts=tb, history=False)
+    assert ierr == 0
+    assert (ta.nstep, ta.time, ta.dt) == (tb.nstep, tb.time, tb.dt)
+    sa.sync_to_host(0)
+    sb.sync_to_host(0)
+    assert not compare(pa, pb, exact=True)
+
+
+def test_hourglass_sedov_reaches_end_time():
+    """The benchmark's workload at a small size: Sedov with the reference's
+    hourglass filter runs to t = 1 on the device loop (300 steps), ending in
+    the CPU restatement's state bit for bit."""
+    from oracle.oracle import Oracle
+    base = Problem.from_deck(configs.sedov(32, kappa=0.01))
+    pg, pc = base.copy(), base.copy()
+    s = Solver(pg, fp_mode=abi.FP_EXACT)
+    ierr, hist = s.run()
+    assert ierr == 0, s.error.message
+    assert pg.timestep.time >= 1.0
+    s.sync_to_host(0)
+    o = Oracle(pc)
+    ierr, n = o.run(pc.timestep)
+    assert ierr == 0 and n == len(hist)
+    assert not compare(pg, pc, exact=True)
+
+
 def test_device_loop_step_limit_and_resume():
     base = Problem.from_deck(configs.noh(20, time_end=0.05, eulerian=True))
     pa, pb = base.copy(), base.copy()
