@@ -68,10 +68,10 @@ __device__ __forceinline__ void elvl_pair(int iel, int i1, const int* nb, const 
   double w6 = r4 + cget(cnbasis, iel1, j2) + cget(cnbasis, iel1, (j2 + 1) & 3);
   double w1 = rv - elvar[iel2];
   double w2 = elvar[iel1] - rv;
-  double w3 = fabs(w1), w4 = fabs(w2);
-  double w7 = copysign(1.0, w2);
+  double w3 = absF(w1), w4 = absF(w2);
+  double w7 = signF(1.0, w2);
   double w8 = DIV(w1 * w6 * w6 + w2 * w5 * w5, w5 * w6 * (w5 + w6));
-  double grad = w7 * minF(minF(fabs(w8), DIV(w3, w5)), DIV(w4, w6));
+  double grad = w7 * minF(minF(absF(w8), DIV(w3, w5)), DIV(w4, w6));
   if (geF(0.0, w1 * w2)) grad = 0.0;
   o1 = r1 * (rv + grad * (r3 - 0.5 * r1));
   o2 = r2 * (rv - grad * (r4 - 0.5 * r2));
@@ -237,10 +237,10 @@ __global__ void __launch_bounds__(BS) k_ale_el(DevFields F, DevCfg C) {
           double rv = cvar[ilndl];
           double w1 = rv - nvar[mm[lnl]];
           double w2 = cvar[ilndr] - rv;
-          double w3 = fabs(w1), w4 = fabs(w2);
-          double w7 = copysign(1.0, w2);
+          double w3 = absF(w1), w4 = absF(w2);
+          double w7 = signF(1.0, w2);
           double w8 = DIV(w2 * w6 * w6 + w1 * w5 * w5, den);
-          double grad = w7 * minF(minF(fabs(w8), DIV(w3, w6)), DIV(w4, w5));
+          double grad = w7 * minF(minF(absF(w8), DIV(w3, w6)), DIV(w4, w5));
           if (geF(0.0, w1 * w2)) grad = 0.0;
           double rd = cdb * (rv + grad * rd0);
           if (q == 0) rdu = rd; else rdv = rd;
@@ -262,10 +262,10 @@ __global__ void __launch_bounds__(BS) k_ale_el(DevFields F, DevCfg C) {
           double rv = cvar[ilndr];
           double w1 = rv - cvar[ilndl];
           double w2 = nvar[mm[lnr]] - rv;
-          double w3 = fabs(w1), w4 = fabs(w2);
-          double w7 = copysign(1.0, w2);
+          double w3 = absF(w1), w4 = absF(w2);
+          double w7 = signF(1.0, w2);
           double w8 = DIV(w1 * w6 * w6 + w2 * w5 * w5, den);
-          double grad = -(w7 * minF(minF(fabs(w8), DIV(w3, w5)), DIV(w4, w6)));
+          double grad = -(w7 * minF(minF(absF(w8), DIV(w3, w5)), DIV(w4, w6)));
           if (geF(0.0, w1 * w2)) grad = 0.0;
           double rd = cdb * (rv + grad * rd0);
           if (q == 0) rdu = rd; else rdv = rd;

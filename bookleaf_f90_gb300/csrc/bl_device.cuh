@@ -125,8 +125,8 @@ __device__ __forceinline__ double minF(double a, double b) { return gtF(a, b) ? 
 // an absolute value, a sum of squares): of a for maxF_nn, of b for minF_nn
 __device__ __forceinline__ double maxF_nn(double a, double b) { return gt_nn(b, a) ? b : a; }
 __device__ __forceinline__ double minF_nn(double a, double b) { return gt_nn(a, b) ? b : a; }
-// Fortran SIGN(a,b): |a| with the sign bit of b (negative zero honoured).
-__device__ __forceinline__ double signF(double a, double b) { return copysign(fabs(a), b); }
+// Fortran SIGN(a,b): |a| with the sign bit of b (negative zero honoured);
+// signF itself is in bl_fp64.cuh, a sign-bit operation.
 
 __device__ __forceinline__ int fc_of(int packed, int j) { return (packed >> (8 * j)) & 0xff; }
 

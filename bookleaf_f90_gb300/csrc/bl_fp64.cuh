@@ -36,10 +36,12 @@
 //   S1 <= S <= S1 + 2.  Rounding as for the divide (no ties exist for a
 //   square root), with the exact remainder N - S^2 near the boundary.
 //
-// Zero operands are answered inline (a signed zero); subnormal, infinite and
-// NaN operands, zero divisors, and quotients whose exponent could leave the
-// normal range take the hardware path, which returns the identical result.  bl_selftest_fp64 checks both routines against the
-// hardware bit for bit on the device.
+// Zero and subnormal operands are handled inline (a signed zero, or the
+// significand normalised with an extended exponent); infinite and NaN
+// operands, zero divisors, and quotients whose exponent could leave the
+// normal range take the hardware path, which returns the identical result.
+// bl_selftest_fp64 checks both routines against the hardware bit for bit on
+// the device.
 //
 // Comparisons: an FP64 comparison is decided on the integer pipe through an
 // order key (the bit pattern for sign-clear values, its reflection for
@@ -120,19 +122,35 @@ static __device__ __noinline__ uint64_t ddiv_fix(uint64_t N, uint64_t D, uint64_
 __device__ __forceinline__ double ddiv_rn(double a, double b) {
   const uint64_t ua = (uint64_t)__double_as_longlong(a);
   const uint64_t ub = (uint64_t)__double_as_longlong(b);
-  const int ea = (int)((ua >> 52) & 0x7FF);
-  const int eb = (int)((ub >> 52) & 0x7FF);
-  const int ed = ea - eb;
-  if ((unsigned)(ea - 1) >= 2046u || (unsigned)(eb - 1) >= 2046u || (unsigned)(ed + 1021) > 2043u) {
-    // a zero dividend over a normal divisor (common: fluid at rest) is the
-    // zero with the product of the signs; the rest is rare
-    if ((ua << 1) == 0 && (unsigned)(eb - 1) < 2046u)
-      return __longlong_as_double((long long)((ua ^ ub) & 0x8000000000000000ull));
-    return a / b;
-  }
   const uint64_t M52 = (1ull << 52) - 1;
-  const uint64_t ma = (ua & M52) | (1ull << 52);
-  const uint64_t mb = (ub & M52) | (1ull << 52);
+  int ea = (int)((ua >> 52) & 0x7FF);
+  int eb = (int)((ub >> 52) & 0x7FF);
+  uint64_t ma = (ua & M52) | (1ull << 52);
+  uint64_t mb = (ub & M52) | (1ull << 52);
+  int ed = ea - eb;
+  if ((unsigned)(ea - 1) >= 2046u || (unsigned)(eb - 1) >= 2046u || (unsigned)(ed + 1021) > 2043u) {
+    const bool az = (ua << 1) == 0, bz = (ub << 1) == 0;
+    // infinities, NaNs and zero divisors: the hardware
+    if (ea == 2047 || eb == 2047 || bz) return a / b;
+    // a zero dividend (common: fluid at rest) gives the zero with the
+    // product of the signs
+    if (az) return __longlong_as_double((long long)((ua ^ ub) & 0x8000000000000000ull));
+    // subnormal operands (tiny velocity differences ahead of a shock) are
+    // normalised, their exponent extended below 1
+    if (ea == 0) {
+      const int s = __clzll((long long)(ua & M52)) - 11;
+      ma = (ua & M52) << s;
+      ea = 1 - s;
+    }
+    if (eb == 0) {
+      const int s = __clzll((long long)(ub & M52)) - 11;
+      mb = (ub & M52) << s;
+      eb = 1 - s;
+    }
+    ed = ea - eb;
+    // a quotient that may be subnormal or overflow: the hardware
+    if ((unsigned)(ed + 1021) > 2043u) return a / b;
+  }
   const bool ge = ma >= mb;
   const uint64_t N = ma << (ge ? 10 : 11);
   const uint64_t D = mb << 11;
@@ -170,12 +188,20 @@ static __device__ __noinline__ uint64_t dsqrt_fix(uint64_t Nhi, uint64_t S) {
 
 __device__ __forceinline__ double dsqrt_rn(double x) {
   const uint64_t ux = (uint64_t)__double_as_longlong(x);
-  const int ex = (int)(ux >> 52);  // with the sign bit: negative x fails the test
-  if ((unsigned)(ex - 1) >= 2046u) return (ux << 1) == 0 ? x : sqrt(x);  // sqrt(+-0) = +-0
   const uint64_t M52 = (1ull << 52) - 1;
-  const int u = ex - 1023;
+  const int ex = (int)(ux >> 52);  // with the sign bit: negative x fails the test
+  uint64_t M = (ux & M52) | (1ull << 52);
+  int u = ex - 1023;
+  if ((unsigned)(ex - 1) >= 2046u) {
+    if ((ux << 1) == 0) return x;  // sqrt(+-0) = +-0
+    if (ex != 0) return sqrt(x);   // negative, infinite, NaN
+    // positive subnormal: normalise (its square root is a normal number)
+    const int s = __clzll((long long)ux) - 11;
+    M = ux << s;
+    u = -1022 - s;
+  }
   const int odd = u & 1;
-  const uint64_t Nhi = ((ux & M52) | (1ull << 52)) << (10 + odd);
+  const uint64_t Nhi = M << (10 + odd);
   const int E = ((u - odd) >> 1) + 1023;
   // seed: r = rsqrt(top 24 bits of Nhi) in (2^-12, 2^-11]; Y0 = r * 2^35,
   // R0 = Y0 * 2^40 ~ 2^127 / sqrt(N)
@@ -218,6 +244,19 @@ __device__ __forceinline__ double dsqrt_rn(double x) {
   if ((L + 3u >= 0x400u && L <= 0x400u) || L + 3u > 0x7FFu) sig = dsqrt_fix(Nhi, S);
   else sig = (S >> 11) + (L > 0x400u ? 1ull : 0ull);
   return __longlong_as_double((long long)(((uint64_t)(E - 1) << 52) + sig));
+}
+
+// ------------------------------------------------------------ sign bits
+
+// |x| and Fortran SIGN(|a|, b) as operations on the sign bit of the high
+// word (integer pipe); an FP64 abs or negate that the compiler cannot fold
+// into a neighbouring instruction would otherwise occupy an FP64 issue slot.
+__device__ __forceinline__ double absF(double x) {
+  return __hiloint2double(__double2hiint(x) & 0x7FFFFFFF, __double2loint(x));
+}
+__device__ __forceinline__ double signF(double a, double b) {
+  return __hiloint2double((__double2hiint(a) & 0x7FFFFFFF) | (__double2hiint(b) & (int)0x80000000),
+                          __double2loint(a));
 }
 
 // ------------------------------------------------------------ comparisons

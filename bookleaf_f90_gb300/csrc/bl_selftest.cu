@@ -5,7 +5,7 @@
 // operand pairs from a counter-based generator (splitmix64 of seed and the
 // index), mixes in hand-picked hard cases (all-ones and all-zeros
 // significands, ratios next to 1, exponent-range edges, zeros, infinities,
-// NaNs, subnormals) and counts results that differ from the hardware in any
+// NaNs, subnormals of every width) and counts results that differ from the hardware in any
 // bit (two NaNs compare equal).  op 0 is the divide, op 1 the square root
 // (its operand is the first of the pair; for op 1 the second reports 0).
 #include <cuda_runtime.h>
@@ -46,6 +46,11 @@ __device__ double pick(uint64_t r, uint64_t r2) {
   else e = 1023;
   if (e < 0) e = 0;
   if (e > 2047) e = 2047;
+  if (kind == 4) {  // subnormal, with a significand of 1..52 bits
+    e = 0;
+    mant = (r & M52) >> ((r2 >> 40) % 52);
+    if (mant == 0) mant = 1;
+  }
   return __longlong_as_double((long long)((sign << 63) | ((uint64_t)e << 52) | mant));
 }
 

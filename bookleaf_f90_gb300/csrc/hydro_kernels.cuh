@@ -72,7 +72,7 @@ __device__ __forceinline__ void eos_pc(const DevCfg& C, int mat, double rho, dou
     double t5 = (1.0 - DIV(__ldg(P), t2)) * __ldg(P + 2) * exp(-t2);
     p = t3 + t4 + t5;
     double pp = p;
-    if (gt_nn(C.pcut, fabs(pp))) pp = 0.0;
+    if (gt_nn(C.pcut, absF(pp))) pp = 0.0;
     double q1 = DIV(__ldg(P + 5), rho);
     double s3 = __ldg(P + 3) * q1;
     double u4 = DIV(__ldg(P), __ldg(P + 3)) + __ldg(P) * q1 - s3 * q1;
@@ -85,7 +85,7 @@ __device__ __forceinline__ void eos_pc(const DevCfg& C, int mat, double rho, dou
     p = -1.0;
     cs2 = C.ccut;
   }
-  if (gt_nn(C.pcut, fabs(p))) p = 0.0;
+  if (gt_nn(C.pcut, absF(p))) p = 0.0;
   cs2 = maxF(cs2, C.ccut);
 }
 
@@ -363,8 +363,8 @@ __global__ void __launch_bounds__(BS, 4) k_getdt(DevFields F, DevCfg C) {
           xh[is] = xhat;
           yh[is] = yhat;
           den = w3 * xhat + w4 * yhat;
-          w1 = DIV(w1 * uhat + w2 * vhat, signF(maxF_nn(fabs(den), zc), den));
-          w1 = DIV(1.0, signF(maxF_nn(fabs(w1), zc), w1));
+          w1 = DIV(w1 * uhat + w2 * vhat, signF(maxF_nn(absF(den), zc), den));
+          w1 = DIV(1.0, signF(maxF_nn(absF(w1), zc), w1));
           // neighbour faces: edge 1 uses MOD(ielfc,4)+1 / MOD(ielfc+2,4)+1,
           // edge 2 the other pair (hydro_kn_edgeviscosity.f90:117-151)
           const int ins1 = e2 == 0 ? ((f1 + 1) & 3) : ((f1 + 3) & 3);
@@ -377,7 +377,7 @@ __global__ void __launch_bounds__(BS, 4) k_getdt(DevFields F, DevCfg C) {
             double ddx = F.ndx[b] - F.ndx[a], ddy = F.ndy[b] - F.ndy[a];
             double ddu = F.ndu[b] - F.ndu[a], ddv = F.ndv[b] - F.ndv[a];
             double dn = ddx * xhat + ddy * yhat;
-            double q = DIV(ddu * uhat + ddv * vhat, signF(maxF_nn(fabs(dn), zc), dn));
+            double q = DIV(ddu * uhat + ddv * vhat, signF(maxF_nn(absF(dn), zc), dn));
             r1 = q * w1;
           }
           if (in2 != iel) {
@@ -387,7 +387,7 @@ __global__ void __launch_bounds__(BS, 4) k_getdt(DevFields F, DevCfg C) {
             double ddx = F.ndx[b] - F.ndx[a], ddy = F.ndy[b] - F.ndy[a];
             double ddu = F.ndu[b] - F.ndu[a], ddv = F.ndv[b] - F.ndv[a];
             double dn = ddx * xhat + ddy * yhat;
-            double q = DIV(ddu * uhat + ddv * vhat, signF(maxF_nn(fabs(dn), zc), dn));
+            double q = DIV(ddu * uhat + ddv * vhat, signF(maxF_nn(absF(dn), zc), dn));
             r2 = q * w1;
           }
           sc[is][0] = r1;
@@ -494,7 +494,7 @@ __global__ void __launch_bounds__(BS, 4) k_getdt(DevFields F, DevCfg C) {
     const double A1 = F.a1[iel], A3 = F.a3[iel], B1 = F.b1[iel], B3 = F.b3[iel];
     double w1 = u[0] * (-B3 + B1) + v[0] * (A3 - A1) + u[1] * (B3 + B1) + v[1] * (-A3 - A1) +
                 u[2] * (B3 - B1) + v[2] * (-A3 + A1) + u[3] * (-B3 - B1) + v[3] * (A3 + A1);
-    w1 = DIV(fabs(w1), F.vol[iel]);
+    w1 = DIV(absF(w1), F.vol[iel]);
     if (gt_nn(w1, divv)) {  // divv is TINY or a larger positive value
       divv = w1;
       divi = iel;

@@ -84,13 +84,19 @@ def sod_reference(nx=100, ny=10, time_end=20.0, eulerian=False):
     return sod(nx, ny, time_end=time_end, eulerian=eulerian, scale=100.0)
 
 
-def sedov(n=512, time_end=1.0, eulerian=False, gamma=1.4, energy=0.244816, kappa=None):
+def sedov(n=512, time_end=1.0, eulerian=False, gamma=1.4, energy=0.244816, kappa=None,
+          pmerit=None):
     """Sedov blast on the quarter domain [0,1.2]^2.  ``kappa`` adds the
     hourglass filter (kappaall) that the reference's own Sedov decks set
-    (input/sedov_lag_small: 0.01); without it the Lagrangian mesh tangles at
-    the origin long before t = 1 and the run stops on dt < dt_min."""
+    (input/sedov_lag_small: 0.01), ``pmerit`` the sub-zonal pressure force
+    (pmeritall).  Without them the Lagrangian mesh tangles at the origin
+    long before t = 1 and the run stops on dt < dt_min; at 512x512 the
+    hourglass filter alone is not enough (stops at t = 0.18), with
+    pmeritall=0.1 as well the run reaches t = 1 in 2,800 steps."""
     ale = "&ALE\n zeul=.TRUE.\n/\n" if eulerian else ""
     hg = "" if kappa is None else f" kappaall={kappa!r}\n"
+    if pmerit is not None:
+        hg += f" pmeritall={pmerit!r}\n"
     return f"""&CONTROL
  time_start=0.0
  time_end={time_end!r}

@@ -133,11 +133,11 @@ def test_restart_from_host_state():
 
 
 def test_hourglass_sedov_reaches_end_time():
-    """The benchmark's workload at a small size: Sedov with the reference's
-    hourglass filter runs to t = 1 on the device loop (300 steps), ending in
-    the CPU restatement's state bit for bit."""
+    """The benchmark's workload at a small size: Sedov with the hourglass
+    filter and sub-zonal pressures runs to t = 1 on the device loop, ending
+    in the CPU restatement's state bit for bit."""
     from oracle.oracle import Oracle
-    base = Problem.from_deck(configs.sedov(32, kappa=0.01))
+    base = Problem.from_deck(configs.sedov(32, kappa=0.01, pmerit=0.1))
     pg, pc = base.copy(), base.copy()
     s = Solver(pg, fp_mode=abi.FP_EXACT)
     ierr, hist = s.run()
