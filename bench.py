@@ -197,7 +197,7 @@ def main():
         cores = os.cpu_count() or 1
         rate, steps, t = cpu_baseline(deck, nel, target_s=20.0, cores=cores)
         line = {"impl": "reference", "metric": "zone-cycles/s FP64", "value": rate,
-                "unit": "zone-cycles/s", "n_gpus": args.gpus, "steps": args.steps,
+                "unit": "zone-cycles/s", "n_gpus": args.gpus, "steps": steps,
                 "warmup": args.warmup, "higher_is_better": True, "dtype": "f64",
                 "data": "synthetic", "config": {"workload": wname, "nel": nel},
                 "cpu_baseline": {"value": rate, "unit": "zone-cycles/s", "cores": cores,

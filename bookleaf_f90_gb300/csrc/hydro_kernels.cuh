@@ -41,6 +41,15 @@
 #define SQRT(a) ::bl::dsqrt_rn(a)
 #endif
 
+// Resident blocks of 128 threads per SM the two heaviest kernels are
+// compiled for (register budget 65536 / (128 * n) per thread).
+#ifndef BL_GETDT_MINB
+#define BL_GETDT_MINB 4
+#endif
+#ifndef BL_FORCE_MINB
+#define BL_FORCE_MINB 4
+#endif
+
 namespace bl {
 namespace BL_NS {
 
@@ -296,7 +305,7 @@ __device__ __forceinline__ void div_max(double& v, int& i, double ov, int oi) {
 }
 
 template <int BS>
-__global__ void __launch_bounds__(BS, 4) k_getdt(DevFields F, DevCfg C) {
+__global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg C) {
   DevStep* S = F.step;
   if (halted(S)) return;
   if (S->stop_next) {            // bl_run: the previous step reached time_end
@@ -620,7 +629,7 @@ __global__ void __launch_bounds__(BS, 4) k_getdt(DevFields F, DevCfg C) {
 // ================================================================ k_lag_force
 
 template <int BS>
-__global__ void __launch_bounds__(BS, 4) k_lag_force(DevFields F, DevCfg C) {
+__global__ void __launch_bounds__(BS, BL_FORCE_MINB) k_lag_force(DevFields F, DevCfg C) {
   const DevStep* S = F.step;
   if (halted(S)) return;
   const int iel = blockIdx.x * BS + threadIdx.x;
