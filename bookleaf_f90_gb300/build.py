@@ -1,9 +1,12 @@
 """Build the sm_103a shared library libbookleaf_gb300.so in-tree.
 
-Three translation units, compiled in parallel with nvcc:
-  bl_kernels.cu  -DBL_NS=fast  --fmad=true   (fused multiply-add allowed)
+Five translation units, compiled in parallel with nvcc:
+  bl_kernels.cu  -DBL_NS=fast  --fmad=true   (fused multiply-add and exact
+                 -DBL_FAST_ALGEBRA=1          algebraic identities allowed)
   bl_kernels.cu  -DBL_NS=exact --fmad=false  (bit-reproducible path)
   bl_capi.cu                                  (the C-ABI, host code)
+  bl_noalloc.cu                               (allocation-free getdt)
+  bl_selftest.cu                              (FP64 self-test and rates)
 and linked with the CUDA runtime statically, so the library needs nothing
 but the driver at run time.
 """
@@ -43,7 +46,8 @@ def build(force=False, verbose=False, extra=()):
     common = [cc] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                             "-Xptxas", "-v" if verbose else "-O3"] + list(extra)
     jobs = [
-        (common + ["--fmad=true", "-DBL_NS=fast", "-c", os.path.join(CSRC, "bl_kernels.cu"),
+        (common + ["--fmad=true", "-DBL_NS=fast", "-DBL_FAST_ALGEBRA=1", "-c",
+                   os.path.join(CSRC, "bl_kernels.cu"),
                    "-o", os.path.join(BUILD, "k_fast.o")]),
         (common + ["--fmad=false", "-DBL_NS=exact", "-c", os.path.join(CSRC, "bl_kernels.cu"),
                    "-o", os.path.join(BUILD, "k_exact.o")]),

@@ -46,6 +46,12 @@
 #ifndef BL_GETDT_MINB
 #define BL_GETDT_MINB 4
 #endif
+// The fast build may also use exact algebraic identities that can change
+// only the sign of a zero (negation symmetry of opposite corners); the
+// exact build evaluates every expression as written.
+#ifndef BL_FAST_ALGEBRA
+#define BL_FAST_ALGEBRA 0
+#endif
 #ifndef BL_FORCE_MINB
 #define BL_FORCE_MINB 4
 #endif
@@ -186,6 +192,19 @@ __device__ __forceinline__ double min_dlm(const double* x, const double* y) {
 __device__ __forceinline__ void force_pq(double p, double a1, double a3, double b1, double b3,
                                          const d4& qx, const d4& qy, double* fx,
                                          double* fy) {
+#if BL_FAST_ALGEBRA
+  // opposite corners carry opposite coefficients: b3 - b1 = -(-b3 + b1)
+  // exactly, up to the sign of a zero
+  const double cb0 = -b3 + b1, cb1 = b3 + b1, ca0 = a3 - a1, ca1 = -a3 - a1;
+  fx[0] = p * cb0;
+  fx[1] = p * cb1;
+  fx[2] = p * -cb0;
+  fx[3] = p * -cb1;
+  fy[0] = p * ca0;
+  fy[1] = p * ca1;
+  fy[2] = p * -ca0;
+  fy[3] = p * -ca1;
+#else
   fx[0] = p * (-b3 + b1);
   fx[1] = p * (b3 + b1);
   fx[2] = p * (b3 - b1);
@@ -194,6 +213,7 @@ __device__ __forceinline__ void force_pq(double p, double a1, double a3, double 
   fy[1] = p * (-a3 - a1);
   fy[2] = p * (-a3 + a1);
   fy[3] = p * (a3 + a1);
+#endif
   fx[0] = fx[0] + qx.x;
   fy[0] = fy[0] + qy.x;
   fx[1] = fx[1] + qx.y;
@@ -209,14 +229,20 @@ __device__ void force_sp(double w1, double rho, double cs2, const double* cx, co
                          const d4& spm, double* fx, double* fy) {
   double x3 = 0.25 * (cx[0] + cx[1] + cx[2] + cx[3]);
   double y3 = 0.25 * (cy[0] + cy[1] + cy[2] + cy[3]);
+  // edge midpoints: x2 of corner j and x4 of corner j+1 are the same sum
+  // (IEEE addition commutes), so each is evaluated once
+  double mx[4], my[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    mx[j] = 0.5 * (cx[j] + cx[(j + 1) & 3]);
+    my[j] = 0.5 * (cy[j] + cy[(j + 1) & 3]);
+  }
   double lfx[4][4], lfy[4][4];
 #pragma unroll
   for (int j1 = 0; j1 < 4; j1++) {
     double x1 = cx[j1], y1 = cy[j1];
-    int j2 = (j1 + 1) & 3;
-    double x2 = 0.5 * (x1 + cx[j2]), y2 = 0.5 * (y1 + cy[j2]);
-    j2 = (j1 + 3) & 3;
-    double x4 = 0.5 * (x1 + cx[j2]), y4 = 0.5 * (y1 + cy[j2]);
+    double x2 = mx[j1], y2 = my[j1];
+    double x4 = mx[(j1 + 3) & 3], y4 = my[(j1 + 3) & 3];
     double w3 = 0.25 * (-x1 + x2 + x3 - x4);
     double w4 = 0.25 * (-x1 - x2 + x3 + x4);
     double w5 = 0.25 * (-y1 + y2 + y3 - y4);
@@ -225,6 +251,18 @@ __device__ void force_sp(double w1, double rho, double cs2, const double* cx, co
     w2 = DIV(c4(spm, j1), w2);
     w2 = w2 - rho;
     w2 = cs2 * w2;
+#if BL_FAST_ALGEBRA
+    // -w5 + w6 = -(w5 - w6) and -w5 - w6 = -(w5 + w6) exactly, up to the
+    // sign of a zero: half the products
+    lfx[j1][0] = w2 * (w5 - w6);
+    lfx[j1][1] = w2 * (w5 + w6);
+    lfx[j1][2] = -lfx[j1][0];
+    lfx[j1][3] = -lfx[j1][1];
+    lfy[j1][0] = w2 * (-w3 + w4);
+    lfy[j1][1] = w2 * (-w3 - w4);
+    lfy[j1][2] = -lfy[j1][0];
+    lfy[j1][3] = -lfy[j1][1];
+#else
     lfx[j1][0] = w2 * (w5 - w6);
     lfx[j1][1] = w2 * (w5 + w6);
     lfx[j1][2] = w2 * (-w5 + w6);
@@ -233,6 +271,7 @@ __device__ void force_sp(double w1, double rho, double cs2, const double* cx, co
     lfy[j1][1] = w2 * (-w3 - w4);
     lfy[j1][2] = w2 * (w3 - w4);
     lfy[j1][3] = w2 * (w3 + w4);
+#endif
   }
   double w2 = 0.5 * (lfx[0][3] + lfx[3][1]);
   double w3 = 0.5 * (lfx[0][1] + lfx[1][3]);

@@ -41,7 +41,8 @@ def test_exact_per_phase(name):
     assert not bad, "\n".join(bad[:10])
 
 
-@pytest.mark.parametrize("name", ["sod_lag", "sedov_lag", "noh_eul", "sod_multimaterial"])
+@pytest.mark.parametrize("name", ["sod_lag", "sedov_lag", "noh_eul", "sod_multimaterial",
+                                  "hourglass_subzonal"])
 def test_fast_within_tolerance(name):
     deck, n = CASES[name]
     pg, pc, bad = run_pair(deck, n, exact=False, phases=False, rtol=1e-9, atol=1e-12)
@@ -148,6 +149,30 @@ def test_hourglass_sedov_reaches_end_time():
     ierr, n = o.run(pc.timestep)
     assert ierr == 0 and n == len(hist)
     assert not compare(pg, pc, exact=True)
+
+
+def test_fast_bench_workload_to_end_time():
+    """Fast mode (the benchmark's mode) over the whole run of the benchmark's
+    workload at 32x32: final totals and fields within the stated tolerances
+    of the CPU restatement."""
+    from oracle.oracle import Oracle
+    base = Problem.from_deck(configs.sedov(32, kappa=0.01, pmerit=0.1))
+    pg, pc = base.copy(), base.copy()
+    s = Solver(pg, fp_mode=abi.FP_FAST)
+    ierr, hist = s.run()
+    assert ierr == 0, s.error.message
+    s.sync_to_host(0)
+    o = Oracle(pc)
+    ierr, n = o.run(pc.timestep)
+    assert ierr == 0 and n == len(hist)
+    tg, tc = pg.totals(), pc.totals()
+    assert abs(tg["mass"] - tc["mass"]) <= 1e-12 * abs(tc["mass"])
+    et, ec = tg["ie"] + tg["ke"], tc["ie"] + tc["ke"]
+    assert abs(et - ec) <= 1e-12 * abs(ec)
+    for fid in (abi.ELDENSITY, abi.ELENERGY, abi.NDU, abi.NDV):
+        a, b = pg.fields[fid], pc.fields[fid]
+        l1 = np.sum(np.abs(a - b)) / max(np.sum(np.abs(b)), 1e-300)
+        assert l1 <= 1e-9, (abi.NAMES[fid], l1)
 
 
 def test_device_loop_step_limit_and_resume():
