@@ -42,9 +42,13 @@
 #endif
 
 // Resident blocks of 128 threads per SM the two heaviest kernels are
-// compiled for (register budget 65536 / (128 * n) per thread).
+// compiled for (register budget 65536 / (128 * n) per thread).  Chosen by
+// timing the whole Sedov 512x512 run on the GB300 over n = 3..6: k_getdt
+// gains from more warps to hide its integer-pipe divide chains (5 blocks,
+// 102 registers), k_lag_force from fewer spills (3 blocks): 414.5M
+// zone-cycles/s against 393.3M with 4 and 4.
 #ifndef BL_GETDT_MINB
-#define BL_GETDT_MINB 4
+#define BL_GETDT_MINB 5
 #endif
 // The fast build may also use exact algebraic identities that can change
 // only the sign of a zero (negation symmetry of opposite corners); the
@@ -53,7 +57,7 @@
 #define BL_FAST_ALGEBRA 0
 #endif
 #ifndef BL_FORCE_MINB
-#define BL_FORCE_MINB 4
+#define BL_FORCE_MINB 3
 #endif
 
 namespace bl {
