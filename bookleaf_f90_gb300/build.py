@@ -9,6 +9,11 @@ Five translation units, compiled in parallel with nvcc:
   bl_selftest.cu                              (FP64 self-test and rates)
 and linked with the CUDA runtime statically, so the library needs nothing
 but the driver at run time.
+
+The C++ host side (host/: control-file reader, mesh generator, initial
+state, solver entry points over the C-ABI) is compiled with g++ alongside
+(-ffp-contract=off, so its set-up arithmetic is the reference's operation
+for operation) and linked into the driver executable _lib/bookleaf_gb300.
 """
 import os
 import shutil
@@ -17,9 +22,12 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
+HOST = os.path.join(HERE, "host")
 OUTDIR = os.path.join(HERE, "_lib")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(OUTDIR, "libbookleaf_gb300.so")
+EXE = os.path.join(OUTDIR, "bookleaf_gb300")
+HOST_SOURCES = ("deck", "mesh", "ic", "problem", "solver", "main")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -32,6 +40,7 @@ def nvcc():
 
 def _sources():
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    deps += [os.path.join(HOST, f) for f in os.listdir(HOST)]
     deps.append(os.path.join(HERE, "..", "include", "bookleaf_gb300.h"))
     return deps
 
@@ -40,7 +49,8 @@ def build(force=False, verbose=False, extra=()):
     os.makedirs(OUTDIR, exist_ok=True)
     os.makedirs(BUILD, exist_ok=True)
     newest = max(os.path.getmtime(p) for p in _sources())
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
+    if (not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest
+            and os.path.exists(EXE) and os.path.getmtime(EXE) >= newest):
         return LIB
     cc = nvcc()
     common = [cc] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -56,6 +66,10 @@ def build(force=False, verbose=False, extra=()):
                    "-o", os.path.join(BUILD, "noalloc.o")]),
         (common + ["-c", os.path.join(CSRC, "bl_selftest.cu"), "-o", os.path.join(BUILD, "selftest.o")]),
     ]
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    for name in HOST_SOURCES:
+        jobs.append([cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-Wall",
+                     "-c", os.path.join(HOST, name + ".cpp"), "-o", os.path.join(BUILD, "h_" + name + ".o")])
     procs = [subprocess.Popen(j, stdout=subprocess.PIPE, stderr=subprocess.STDOUT) for j in jobs]
     logs = []
     for j, p in zip(jobs, procs):
@@ -63,7 +77,7 @@ def build(force=False, verbose=False, extra=()):
         logs.append(out.decode(errors="replace"))
         if p.returncode != 0:
             sys.stderr.write(out.decode(errors="replace"))
-            raise RuntimeError("nvcc failed: " + " ".join(j))
+            raise RuntimeError("compile failed: " + " ".join(j))
     tmp = LIB + ".%d.tmp" % os.getpid()
     subprocess.check_call([cc] + ARCH + ["-shared", "-cudart", "static", "-o", tmp,
                                          os.path.join(BUILD, "k_fast.o"),
@@ -72,6 +86,10 @@ def build(force=False, verbose=False, extra=()):
                                          os.path.join(BUILD, "noalloc.o"),
                                          os.path.join(BUILD, "selftest.o")])
     os.replace(tmp, LIB)
+    tmp = EXE + ".%d.tmp" % os.getpid()
+    subprocess.check_call([cxx, "-o", tmp] + [os.path.join(BUILD, "h_" + n + ".o") for n in HOST_SOURCES]
+                          + ["-L" + OUTDIR, "-lbookleaf_gb300", "-Wl,-rpath,$ORIGIN"])
+    os.replace(tmp, EXE)
     if verbose:
         sys.stdout.write("\n".join(logs))
     return LIB
