@@ -53,6 +53,10 @@ def load(build_if_missing=True):
     L.bl_selftest_fp64.restype = ct.c_int
     L.bl_fp64_rates.argtypes = [P(ct.c_double), ct.c_int]
     L.bl_fp64_rates.restype = ct.c_int
+    L.bl_shortprint.argtypes = [vp, ct.c_int, P(ct.c_double), ct.c_int, P(abi.Error)]
+    L.bl_shortprint.restype = ct.c_int
+    L.bl_check_sod.argtypes = [vp, ct.c_double, P(ct.c_double), P(ct.c_double), P(abi.Error)]
+    L.bl_check_sod.restype = ct.c_int
     L.bl_abi_sizes.argtypes = [P(ct.c_int), ct.c_int]
     L.bl_abi_sizes.restype = ct.c_int
     _lib = L
@@ -63,7 +67,7 @@ def load(build_if_missing=True):
 EXPORTS = ("bl_init", "bl_finalize", "bl_getdt", "bl_lagstep", "bl_alestep", "bl_run",
            "bl_sync_to_host", "bl_sync_to_device", "bl_synchronize", "bl_stream",
            "bl_kernel_launches", "bl_version", "bl_getdt_noalloc", "bl_selftest_fp64",
-           "bl_fp64_rates")
+           "bl_fp64_rates", "bl_shortprint", "bl_check_sod")
 
 
 def fp64_rates():

@@ -16,34 +16,12 @@
 
 #include "../../include/bookleaf_gb300.h"
 #include "bl_device.cuh"
+#include "bl_ctx.h"
 #include "bl_kernels.h"
 
 using bl::DevStep;
 using bl::d4;
 
-struct bl_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  bl_sizes s{};
-  bl_config c{};
-  int fp_mode = BL_FP_FAST;
-  void* host[BL_NID + 1] = {};
-  bl::DevFields F{};
-  bl::DevCfg C{};
-  bl::Launchers L{};
-  std::vector<void*> bufs;
-  DevStep* hstep = nullptr;  // pinned mirror of F.step
-  bool cs2_is_v = false;     // elcs2 currently holds cs2 + elvisc (after getdt)
-  long long launches = 0;
-  // bl_run
-  cudaGraphExec_t gexec = nullptr;
-  int gsteps = 0;
-  bool g_ale = false;
-  bl::StepRec* g_hist = nullptr;  // history buffer and record limit the
-  int g_maxrec = -1;              // graph's kernel arguments were captured with
-  int hist_cap = 0;
-  std::vector<int> ielmat_h;  // for timestep%mdt
-};
 
 namespace {
 
@@ -566,6 +544,7 @@ int bl_finalize(bl_ctx* x) {
   if (x->gexec) cudaGraphExecDestroy(x->gexec);
   for (void* p : x->bufs) cudaFree(p);
   if (x->F.hist) cudaFree(x->F.hist);
+  if (x->diag) cudaFree(x->diag);
   if (x->hstep) cudaFreeHost(x->hstep);
   if (x->stream) cudaStreamDestroy(x->stream);
   delete x;

@@ -1,0 +1,38 @@
+// bl_ctx.h -- the library context behind the opaque bl_ctx of the C-ABI:
+// device mirrors, configuration tables, stream, launchers and the state of
+// the device time loop.  Shared by the C-ABI sources of the library.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "../../include/bookleaf_gb300.h"
+#include "bl_device.cuh"
+#include "bl_kernels.h"
+
+struct bl_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bl_sizes s{};
+  bl_config c{};
+  int fp_mode = BL_FP_FAST;
+  void* host[BL_NID + 1] = {};
+  bl::DevFields F{};
+  bl::DevCfg C{};
+  bl::Launchers L{};
+  std::vector<void*> bufs;
+  bl::DevStep* hstep = nullptr;  // pinned mirror of F.step
+  bool cs2_is_v = false;     // elcs2 currently holds cs2 + elvisc (after getdt)
+  long long launches = 0;
+  // bl_run
+  cudaGraphExec_t gexec = nullptr;
+  int gsteps = 0;
+  bool g_ale = false;
+  bl::StepRec* g_hist = nullptr;  // history buffer and record limit the
+  int g_maxrec = -1;              // graph's kernel arguments were captured with
+  int hist_cap = 0;
+  std::vector<int> ielmat_h;  // for timestep%mdt
+  // diagnostics scratch (bl_shortprint, bl_check_sod), grown on demand
+  double* diag = nullptr;
+  size_t diag_cap = 0;
+};

@@ -102,6 +102,16 @@ std::string read_file(const std::string& path);
 // Set-up dump (tests compare it with the Python harness array by array).
 void write_setup_dump(const Problem& p, const std::string& path);
 
+// hydro_kn_calc_shortprint (hydro_kn_print.F90:52-101) per region or
+// material flag: volume, mass, internal and kinetic energy, mass-weighted
+// pressure, pressure and density extremes (and the averages of
+// hydro_kn_average_shortprint when computed on the device).
+struct FlagTotals {
+  double vol = 0, mass = 0, ie = 0, ke = 0, pressure = 0;
+  double pmn = 0, pmx = 0, dmn = 0, dmx = 0;
+  double density = 0;
+};
+
 // ---------------------------------------------------------------- solver
 
 // Error carried out of a failed entry point: error_t{ierr,iout,serr}.
@@ -130,6 +140,9 @@ class Solver {
   int run(bl_timestep& ts, int max_steps, int* nsteps);
   void sync_to_host(int id = 0);
   void sync_to_device(int id = 0);
+  // diagnostics from the device state (bl_shortprint, bl_check_sod)
+  std::vector<FlagTotals> shortprint(bool by_material);
+  void check_sod(double time, double& l1_density, double& l1_energy);
   const bl_error& error() const { return err_; }
   bl_ctx* ctx() { return ctx_; }
 
@@ -142,15 +155,14 @@ class Solver {
 
 // ---------------------------------------------------------------- reports
 
-// hydro_kn_calc_shortprint (hydro_kn_print.F90:52-101) per region or
-// material flag: volume, mass, internal and kinetic energy, mass-weighted
-// pressure, pressure and density extremes.
-struct FlagTotals {
-  double vol = 0, mass = 0, ie = 0, ke = 0, pressure = 0;
-  double pmn = 0, pmx = 0, dmn = 0, dmx = 0;
-};
+// host-side short print of a Problem's fields (elements only), with the
+// averages of hydro_kn_average_shortprint
 std::vector<FlagTotals> shortprint(const Problem& p, bool by_material);
+// the short print (hydro_kn_write_*_shortprint layout) from host tables
 std::string format_shortprint(const Problem& p, int nstep, double time);
+std::string format_shortprint(const Problem& p, int nstep, double time,
+                              const std::vector<FlagTotals>& regions,
+                              const std::vector<FlagTotals>& materials);
 
 // check_kn_sod (check_kn_tests.f90:33-111): L1 norms of density and energy
 // against the exact Sod solution in the check's geometry (x in [0,100],

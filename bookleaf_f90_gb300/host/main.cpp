@@ -99,7 +99,13 @@ int main(int argc, char** argv) {
   int rc = 0;
   try {
     blh::Solver s(p, fp);
-    std::fputs(blh::format_shortprint(p, p.timestep.nstep, p.timestep.time).c_str(), stdout);
+    // short prints from the device state (bl_shortprint): no field copy
+    auto print = [&](const bl_timestep& t) {
+      std::fputs(blh::format_shortprint(p, t.nstep, t.time, s.shortprint(false), s.shortprint(true))
+                     .c_str(),
+                 stdout);
+    };
+    print(p.timestep);
     bl_timestep& ts = p.timestep;
     const auto t0 = std::chrono::steady_clock::now();
     long nsteps = 0;
@@ -122,20 +128,22 @@ int main(int argc, char** argv) {
       nsteps = n;
     }
     const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-    s.sync_to_host(0);
     if (ierr != BL_SUCCESS) {
       std::printf("\n %s\n", trimmed(s.error().serr, sizeof s.error().serr).c_str());
       rc = 1;
     }
-    std::fputs(blh::format_shortprint(p, ts.nstep, ts.time).c_str(), stdout);
+    print(ts);
     std::printf("\n %ld steps in %.3f s: %.3e zone-cycles/s, grind %.3e us\n", nsteps, el,
                 nsteps * (double)p.sizes.nel / el, el * 1e6 / ((double)nsteps * p.sizes.nel));
     if (deck.find("sod") != std::string::npos) {
       double l1d, l1e;
-      blh::check_sod(p, ts.time, l1d, l1e);
+      s.check_sod(ts.time, l1d, l1e);
       std::printf(" VALIDATION\n  Sod shocktube test case\n   L1 norm. of density: %16.9e\n", l1d);
     }
-    if (!dump_final.empty()) blh::write_setup_dump(p, dump_final);
+    if (!dump_final.empty()) {
+      s.sync_to_host(0);
+      blh::write_setup_dump(p, dump_final);
+    }
   } catch (const blh::SolverError& e) {
     std::fprintf(stderr, "%s\n", e.what());
     return 1;

@@ -190,10 +190,20 @@ std::vector<FlagTotals> shortprint(const Problem& p, bool by_material) {
       }
     }
   }
+  for (auto& f : t) {  // hydro_kn_average_shortprint (hydro_kn_print.F90:219-240)
+    f.density = f.vol > 0.0 ? f.mass / f.vol : 0.0;
+    if (f.mass > dencut * f.vol) f.pressure = f.pressure / f.mass;
+  }
   return t;
 }
 
 std::string format_shortprint(const Problem& p, int nstep, double time) {
+  return format_shortprint(p, nstep, time, shortprint(p, false), shortprint(p, true));
+}
+
+std::string format_shortprint(const Problem& p, int nstep, double time,
+                              const std::vector<FlagTotals>& reg,
+                              const std::vector<FlagTotals>& matl) {
   std::ostringstream o;
   char buf[512];
   std::snprintf(buf, sizeof buf, "\n  Step no. %7d Time = %14.7f\n", nstep, time);
@@ -201,7 +211,7 @@ std::string format_shortprint(const Problem& p, int nstep, double time) {
   double tv = 0, tm = 0, tie = 0, tke = 0, tp = 0;
   for (int pass = 0; pass < 2; pass++) {
     const bool mat = pass == 1;
-    const auto t = shortprint(p, mat);
+    const auto& t = mat ? matl : reg;
     o << "\n" << (mat ? " Material" : " Region") << " summary\n\n";
     std::snprintf(buf, sizeof buf, "  %-10s %11s %11s %11s %11s %11s %11s %11s %11s %11s %11s\n",
                   mat ? "material" : "region", "vol", "mass", "tot ie", "tot ke", "press",
@@ -210,19 +220,17 @@ std::string format_shortprint(const Problem& p, int nstep, double time) {
     const auto& names = mat ? p.material_names : p.region_names;
     for (size_t i = 0; i < t.size(); i++) {
       const auto& f = t[i];
-      const double press = f.mass > 0 ? f.pressure / f.mass : 0.0;
-      const double dens = f.vol > 0 ? f.mass / f.vol : 0.0;
       std::snprintf(buf, sizeof buf,
                     "  %-10.10s %11.4e %11.4e %11.4e %11.4e %11.4e %11.4e %11.4e %11.4e %11.4e %11.4e\n",
-                    i < names.size() ? names[i].c_str() : "", f.vol, f.mass, f.ie, f.ke, press,
-                    f.pmn, f.pmx, dens, f.dmn, f.dmx);
+                    i < names.size() ? names[i].c_str() : "", f.vol, f.mass, f.ie, f.ke,
+                    f.pressure, f.pmn, f.pmx, f.density, f.dmn, f.dmx);
       o << buf;
       if (!mat) {
         tv += f.vol;
         tm += f.mass;
         tie += f.ie;
         tke += f.ke;
-        tp += f.pressure;
+        tp += f.pressure * f.mass;
       }
     }
   }

@@ -42,4 +42,31 @@ void Solver::sync_to_device(int id) {
     throw SolverError(BL_FAILURE, BL_HALT_ALL, "bl_sync_to_device failed");
 }
 
+std::vector<FlagTotals> Solver::shortprint(bool by_material) {
+  const int n = by_material ? p_.sizes.nmat : p_.sizes.nreg;
+  std::vector<double> out((size_t)n * BL_SP_NQ);
+  if (bl_shortprint(ctx_, by_material ? 1 : 0, out.data(), n, &err_) != BL_SUCCESS)
+    throw SolverError(err_.ierr, err_.iout, err_.serr);
+  std::vector<FlagTotals> t(n);
+  for (int i = 0; i < n; i++) {
+    const double* r = &out[(size_t)i * BL_SP_NQ];
+    t[i].vol = r[0];
+    t[i].mass = r[1];
+    t[i].ie = r[2];
+    t[i].ke = r[3];
+    t[i].pressure = r[4];
+    t[i].pmn = r[5];
+    t[i].pmx = r[6];
+    t[i].density = r[7];
+    t[i].dmn = r[8];
+    t[i].dmx = r[9];
+  }
+  return t;
+}
+
+void Solver::check_sod(double time, double& l1_density, double& l1_energy) {
+  if (bl_check_sod(ctx_, time, &l1_density, &l1_energy, &err_) != BL_SUCCESS)
+    throw SolverError(err_.ierr, err_.iout, err_.serr);
+}
+
 }  // namespace blh

@@ -79,6 +79,27 @@ class Solver:
                 recs.append((r.nstep, r.time, r.dt, r.idtel, abi.DT_NAMES[r.sdt_code]))
         return ierr, recs
 
+    # ---- diagnostics on the device -------------------------------------------
+    SHORTPRINT_COLUMNS = ("vol", "mass", "ie", "ke", "pressure", "pmn", "pmx", "density",
+                          "dmn", "dmx")
+
+    def shortprint(self, by_material=False):
+        """hydro_dr_shortprint's per-region (or per-material) table from the
+        device state: a list of dicts with SHORTPRINT_COLUMNS."""
+        n = self.problem.sizes.nmat if by_material else self.problem.sizes.nreg
+        out = (ct.c_double * (n * 10))()
+        if self.L.bl_shortprint(self.ctx, int(by_material), out, n, ct.byref(self.error)) != 0:
+            raise SolverError(-1, self.error.iout, self.error.message)
+        return [dict(zip(self.SHORTPRINT_COLUMNS, out[10 * i:10 * i + 10])) for i in range(n)]
+
+    def check_sod(self, time=None):
+        """check_dr_sod on the device: (density L1, energy L1)."""
+        t = self.timestep.time if time is None else time
+        d, e = ct.c_double(), ct.c_double()
+        if self.L.bl_check_sod(self.ctx, t, ct.byref(d), ct.byref(e), ct.byref(self.error)) != 0:
+            raise SolverError(-1, self.error.iout, self.error.message)
+        return d.value, e.value
+
     # ---- data movement ------------------------------------------------------
     def sync_to_host(self, fid=0):
         if self.L.bl_sync_to_host(self.ctx, int(fid)) != 0:

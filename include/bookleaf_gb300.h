@@ -227,6 +227,29 @@ int bl_selftest_fp64(int op, long long n, unsigned long long seed, long long *mi
  * against.  Returns 0, or -1 when CUDA fails. */
 int bl_fp64_rates(double *rates, int n);
 
+/* ---- diagnostics on the device ------------------------------------------ */
+
+/* Columns of one bl_shortprint row. */
+#define BL_SP_NQ 10
+
+/* hydro_dr_shortprint's reductions (src/packages/hydro/driver/
+ * hydro_dr_print.f90:49-170) from the device state, for a host that prints
+ * the short print without copying the fields back: table 0 per region,
+ * table 1 per material (mixed-cell components included, as
+ * utils_kn_mxgathercncp feeds them).  out receives nflag rows (nflag >=
+ * nreg resp. nmat) of BL_SP_NQ values: volume, mass, internal energy,
+ * kinetic energy, pressure (mass-weighted mean), minimum and maximum
+ * pressure, density (mass/volume), minimum and maximum density.  The sums
+ * are fixed trees, reproducible run to run; they differ from the
+ * reference's serial sums in rounding only. */
+int bl_shortprint(bl_ctx *ctx, int table, double *out, int nflag, bl_error *error);
+
+/* check_dr_sod (src/packages/check/driver/check_dr_tests.f90:34-71) on the
+ * device: L1 norms of density and energy against the exact Sod solution in
+ * the reference check's geometry (interface at x = 50, gamma 1.4). */
+int bl_check_sod(bl_ctx *ctx, double time, double *l1_density, double *l1_energy,
+                 bl_error *error);
+
 /* ---- allocation-free getdt ---------------------------------------------- */
 
 /* Largest mesh bl_getdt_noalloc accepts: its reduction scratch lives in a
