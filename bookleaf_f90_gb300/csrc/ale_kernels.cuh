@@ -48,7 +48,7 @@ __device__ __forceinline__ double face_dv(double x1, double x2, double y1, doubl
   double a3 = (-x1 + x4) + (x3 - x2);
   double b1 = (-y1 - y4) + (y3 + y2);
   double b3 = (-y1 + y4) + (y3 - y2);
-  return 0.25 * (a1 * b3 - a3 * b1);
+  return quarter(a1 * b3 - a3 * b1);
 }
 
 // The limited face flux of ale_kn_fluxelvl for the pair (i1, i2=i1+2),
@@ -73,8 +73,8 @@ __device__ __forceinline__ void elvl_pair(int iel, int i1, const int* nb, const 
   double w8 = DIV(w1 * w6 * w6 + w2 * w5 * w5, w5 * w6 * (w5 + w6));
   double grad = w7 * minF(minF(absF(w8), DIV(w3, w5)), DIV(w4, w6));
   if (geF(0.0, w1 * w2)) grad = 0.0;
-  o1 = r1 * (rv + grad * (r3 - 0.5 * r1));
-  o2 = r2 * (rv - grad * (r4 - 0.5 * r2));
+  o1 = r1 * (rv + grad * (r3 - half(r1)));
+  o2 = r2 * (rv - grad * (r4 - half(r2)));
   (void)iel;
 }
 
@@ -191,10 +191,10 @@ __global__ void __launch_bounds__(BS) k_ale_el(DevFields F, DevCfg C) {
     if (nb[i2] == iel) w4 = 0.0;
     double w1 = w3 - fm[i1];
     double w2 = w4 - fm[i2];
-    w3 = 0.25 * (w1 - w2);
+    w3 = quarter(w1 - w2);
     cndm[i1] = w3;
     cndm[i2] = w3;
-    w3 = 0.25 * (w1 + w2);
+    w3 = quarter(w1 + w2);
     cnfl = cnfl + w3;
   }
   F.cnflux[iel] = make_d4(cnfl, cnfl, cnfl, cnfl);
@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(BS) k_ale_el(DevFields F, DevCfg C) {
         const int lnr = (ifcl - icn + 1) % 4;
         const int4 m = __ldg(F.ielnd + iell);
         const int mm[4] = {m.x, m.y, m.z, m.w};
-        double rd0 = ob[ilndl] - 0.5 * cdb;
+        double rd0 = ob[ilndl] - half(cdb);
         double w5 = ob[ilndl] + ob[ilndr];
         double w6 = cget(F.cnmass, iell, lnl) + cget(F.cnmass, iell, lnr);
         const double den = w5 * w6 * (w5 + w6);
@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(BS) k_ale_el(DevFields F, DevCfg C) {
         const int lnr = (((ifcr - icn - 1) % 4) + 4) % 4;
         const int4 m = __ldg(F.ielnd + ielr);
         const int mm[4] = {m.x, m.y, m.z, m.w};
-        double rd0 = ob[ilndr] + 0.5 * cdb;
+        double rd0 = ob[ilndr] + half(cdb);
         double w5 = ob[ilndl] + ob[ilndr];
         double w6 = cget(F.cnmass, ielr, lnl) + cget(F.cnmass, ielr, lnr);
         const double den = w5 * w6 * (w5 + w6);
@@ -297,7 +297,7 @@ __global__ void __launch_bounds__(BS) k_ale_nd(DevFields F, DevCfg C) {
   for (int k = b; k < e; k++) {
     const int c = __ldg(F.ne_ent + k);
     const int iel = c >> 2, j = c & 3;
-    v0 = v0 + 0.25 * F.vpr[iel];
+    v0 = v0 + quarter(F.vpr[iel]);
     m0 = m0 + cget(F.cnmass, iel, j);
   }
   double m1 = m0;
@@ -389,7 +389,7 @@ __global__ void __launch_bounds__(BS) k_ale_update(DevFields F, DevCfg C) {
     const int c0 = F.imxfcp[imx], nc = F.imxncp[imx];
     for (int k = 0; k < nc; k++) {
       const int icp = c0 + k;
-      const double cpv = 4.0 * (g.a1 * g.b3 - g.a3 * g.b1) * F.frvol[icp];
+      const double cpv = times4(g.a1 * g.b3 - g.a3 * g.b1) * F.frvol[icp];
       const double cpr = DIV(F.cpm[icp], cpv);
       double cpp, cpc;
       eos_pc(C, __ldg(F.icpmat + icp), cpr, F.cpe[icp], cpp, cpc);

@@ -246,6 +246,29 @@ __device__ __forceinline__ double dsqrt_rn(double x) {
   return __longlong_as_double((long long)(((uint64_t)(E - 1) << 52) + sig));
 }
 
+// ------------------------------------------------------------ powers of two
+
+// x * 2^K exactly as the FP64 multiply rounds it, by adding K to the
+// exponent field when x and the product are normal numbers; zeros return
+// themselves, and subnormal, infinite or NaN operands and products that
+// leave the normal range take the FP64 multiply.  The scalings by 0.5,
+// 0.25, 2 and 4 that the reference's formulas are full of then cost no
+// FP64 issue slot.
+static __device__ __noinline__ double ldexp_slow(double x, double s) { return x * s; }
+template <int K>
+__device__ __forceinline__ double ldexpF(double x) {
+  const long long b = __double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7FF);
+  if ((unsigned)(e - 1) < 2046u && (unsigned)(e + K - 1) < 2046u)
+    return __longlong_as_double(b + (long long)((unsigned long long)(long long)K << 52));
+  if (((unsigned long long)b << 1) == 0) return x;
+  return ldexp_slow(x, K >= 0 ? (double)(1 << (K >= 0 ? K : 0)) : 1.0 / (double)(1 << (K < 0 ? -K : 0)));
+}
+__device__ __forceinline__ double half(double x) { return ldexpF<-1>(x); }
+__device__ __forceinline__ double quarter(double x) { return ldexpF<-2>(x); }
+__device__ __forceinline__ double twice(double x) { return ldexpF<1>(x); }
+__device__ __forceinline__ double times4(double x) { return ldexpF<2>(x); }
+
 // ------------------------------------------------------------ sign bits
 
 // |x| and Fortran SIGN(|a|, b) as operations on the sign bit of the high

@@ -116,12 +116,12 @@ struct Iso {
 
 __device__ __forceinline__ Iso getiso(const double* x, const double* y) {
   Iso g;
-  g.a1 = 0.25 * (-x[0] + x[1] + x[2] - x[3]);
-  g.a2 = 0.25 * (x[0] - x[1] + x[2] - x[3]);
-  g.a3 = 0.25 * (-x[0] - x[1] + x[2] + x[3]);
-  g.b1 = 0.25 * (-y[0] + y[1] + y[2] - y[3]);
-  g.b2 = 0.25 * (y[0] - y[1] + y[2] - y[3]);
-  g.b3 = 0.25 * (-y[0] - y[1] + y[2] + y[3]);
+  g.a1 = quarter(-x[0] + x[1] + x[2] - x[3]);
+  g.a2 = quarter(x[0] - x[1] + x[2] - x[3]);
+  g.a3 = quarter(-x[0] - x[1] + x[2] + x[3]);
+  g.b1 = quarter(-y[0] + y[1] + y[2] - y[3]);
+  g.b2 = quarter(y[0] - y[1] + y[2] - y[3]);
+  g.b3 = quarter(-y[0] - y[1] + y[2] + y[3]);
   const double o9 = 1.0 / 9.0;
   const double A1m = 3.0 * g.a1 - g.a2, A1p = 3.0 * g.a1 + g.a2;
   const double A3m = 3.0 * g.a3 - g.a2, A3p = 3.0 * g.a3 + g.a2;
@@ -131,7 +131,7 @@ __device__ __forceinline__ Iso getiso(const double* x, const double* y) {
   g.w1 = o9 * (B3p * A1m - A3p * B1m);
   g.w2 = o9 * (B3p * A1p - A3p * B1p);
   g.w3 = o9 * (B3m * A1p - A3m * B1p);
-  g.vol = 4.0 * (g.a1 * g.b3 - g.a3 * g.b1);
+  g.vol = times4(g.a1 * g.b3 - g.a3 * g.b1);
   return g;
 }
 
@@ -142,13 +142,13 @@ __device__ __forceinline__ double g_denom(double x1, double y1, double x2, doubl
 }
 __device__ __forceinline__ double g_distpp(double x3, double y3, double x4, double y4, double x1,
                                            double y1) {
-  double w1 = 0.5 * (x3 + x4) - x1;
-  double w2 = 0.5 * (y3 + y4) - y1;
+  double w1 = half(x3 + x4) - x1;
+  double w2 = half(y3 + y4) - y1;
   return w1 * w1 + w2 * w2;
 }
 __device__ __forceinline__ double g_distpl(double x3, double y3, double x4, double y4, double x1,
                                            double y1, double x2, double y2) {
-  double res = 0.5 * (y1 - y2) * (x3 + x4) + 0.5 * (y3 + y4) * (x2 - x1) + y2 * x1 - y1 * x2;
+  double res = half(y1 - y2) * (x3 + x4) + half(y3 + y4) * (x2 - x1) + y2 * x1 - y1 * x2;
   return res * res;
 }
 
@@ -174,15 +174,15 @@ __device__ __forceinline__ double min_dln(const double* x, const double* y, doub
 // MINVAL(geometry_kn_dlm(...)) (geometry_kn_length.f90:30-56)
 __device__ __forceinline__ double min_dlm(const double* x, const double* y) {
   double x1 = x[0] + x[1], x2 = x[2] + x[3], y1 = y[0] + y[1], y2 = y[2] + y[3];
-  x1 = 0.5 * (x1 - x2);
-  y1 = 0.5 * (y1 - y2);
+  x1 = half(x1 - x2);
+  y1 = half(y1 - y2);
   double r0 = x1 * x1 + y1 * y1;
   x1 = x[2] + x[1];
   x2 = x[0] + x[3];
   y1 = y[2] + y[1];
   y2 = y[0] + y[3];
-  x1 = 0.5 * (x1 - x2);
-  y1 = 0.5 * (y1 - y2);
+  x1 = half(x1 - x2);
+  y1 = half(y1 - y2);
   double r1 = x1 * x1 + y1 * y1;
   double m = r0;
   m = minF_nn(m, r1);
@@ -231,15 +231,15 @@ __device__ __forceinline__ void force_pq(double p, double a1, double a3, double 
 // hydro_kn_getforceSP (hydro_kn_getforce.f90:109-188)
 __device__ void force_sp(double w1, double rho, double cs2, const double* cx, const double* cy,
                          const d4& spm, double* fx, double* fy) {
-  double x3 = 0.25 * (cx[0] + cx[1] + cx[2] + cx[3]);
-  double y3 = 0.25 * (cy[0] + cy[1] + cy[2] + cy[3]);
+  double x3 = quarter(cx[0] + cx[1] + cx[2] + cx[3]);
+  double y3 = quarter(cy[0] + cy[1] + cy[2] + cy[3]);
   // edge midpoints: x2 of corner j and x4 of corner j+1 are the same sum
   // (IEEE addition commutes), so each is evaluated once
   double mx[4], my[4];
 #pragma unroll
   for (int j = 0; j < 4; j++) {
-    mx[j] = 0.5 * (cx[j] + cx[(j + 1) & 3]);
-    my[j] = 0.5 * (cy[j] + cy[(j + 1) & 3]);
+    mx[j] = half(cx[j] + cx[(j + 1) & 3]);
+    my[j] = half(cy[j] + cy[(j + 1) & 3]);
   }
   double lfx[4][4], lfy[4][4];
 #pragma unroll
@@ -247,11 +247,11 @@ __device__ void force_sp(double w1, double rho, double cs2, const double* cx, co
     double x1 = cx[j1], y1 = cy[j1];
     double x2 = mx[j1], y2 = my[j1];
     double x4 = mx[(j1 + 3) & 3], y4 = my[(j1 + 3) & 3];
-    double w3 = 0.25 * (-x1 + x2 + x3 - x4);
-    double w4 = 0.25 * (-x1 - x2 + x3 + x4);
-    double w5 = 0.25 * (-y1 + y2 + y3 - y4);
-    double w6 = 0.25 * (-y1 - y2 + y3 + y4);
-    double w2 = 4.0 * (w3 * w6 - w4 * w5);
+    double w3 = quarter(-x1 + x2 + x3 - x4);
+    double w4 = quarter(-x1 - x2 + x3 + x4);
+    double w5 = quarter(-y1 + y2 + y3 - y4);
+    double w6 = quarter(-y1 - y2 + y3 + y4);
+    double w2 = times4(w3 * w6 - w4 * w5);
     w2 = DIV(c4(spm, j1), w2);
     w2 = w2 - rho;
     w2 = cs2 * w2;
@@ -277,20 +277,20 @@ __device__ void force_sp(double w1, double rho, double cs2, const double* cx, co
     lfy[j1][3] = w2 * (w3 + w4);
 #endif
   }
-  double w2 = 0.5 * (lfx[0][3] + lfx[3][1]);
-  double w3 = 0.5 * (lfx[0][1] + lfx[1][3]);
-  double w4 = 0.5 * (lfx[1][1] + lfx[2][3]);
-  double w5 = 0.5 * (lfx[3][3] + lfx[2][1]);
-  double w6 = 0.25 * (lfx[0][2] + lfx[1][2] + lfx[2][2] + lfx[3][2]);
+  double w2 = half(lfx[0][3] + lfx[3][1]);
+  double w3 = half(lfx[0][1] + lfx[1][3]);
+  double w4 = half(lfx[1][1] + lfx[2][3]);
+  double w5 = half(lfx[3][3] + lfx[2][1]);
+  double w6 = quarter(lfx[0][2] + lfx[1][2] + lfx[2][2] + lfx[3][2]);
   fx[0] = fx[0] + w1 * (lfx[0][0] + w2 + w3 + w6);
   fx[1] = fx[1] + w1 * (lfx[1][0] + w4 + w3 + w6);
   fx[2] = fx[2] + w1 * (lfx[2][0] + w4 + w5 + w6);
   fx[3] = fx[3] + w1 * (lfx[3][0] + w2 + w5 + w6);
-  w2 = 0.5 * (lfy[0][3] + lfy[3][1]);
-  w3 = 0.5 * (lfy[0][1] + lfy[1][3]);
-  w4 = 0.5 * (lfy[1][1] + lfy[2][3]);
-  w5 = 0.5 * (lfy[3][3] + lfy[2][1]);
-  w6 = 0.25 * (lfy[0][2] + lfy[1][2] + lfy[2][2] + lfy[3][2]);
+  w2 = half(lfy[0][3] + lfy[3][1]);
+  w3 = half(lfy[0][1] + lfy[1][3]);
+  w4 = half(lfy[1][1] + lfy[2][3]);
+  w5 = half(lfy[3][3] + lfy[2][1]);
+  w6 = quarter(lfy[0][2] + lfy[1][2] + lfy[2][2] + lfy[3][2]);
   fy[0] = fy[0] + w1 * (lfy[0][0] + w2 + w3 + w6);
   fy[1] = fy[1] + w1 * (lfy[1][0] + w4 + w3 + w6);
   fy[2] = fy[2] + w1 * (lfy[2][0] + w4 + w5 + w6);
@@ -376,59 +376,65 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
     double visc = 0.0;
     double qx[4] = {0.0, 0.0, 0.0, 0.0}, qy[4] = {0.0, 0.0, 0.0, 0.0};
     if (!C.ztq) {
-      // hydro_kn_initeviscosity: face j runs corner j -> j+1
-      double du[4], dv[4], dx[4], dy[4];
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        const int jn = (j + 1) & 3;
-        du[j] = u[jn] - u[j];
-        dv[j] = v[jn] - v[j];
-        dx[j] = x[jn] - x[j];
-        dy[j] = y[jn] - y[j];
-      }
+      // hydro_kn_initeviscosity / limiteviscosity / geteviscosity
+      // (hydro_kn_edgeviscosity.f90:30-282), evaluated face by face: every
+      // quantity of a face -- its differences (face j runs corner j ->
+      // j+1), lengths, normalised vectors, limiter ratios, edge coefficient
+      // and edge force -- is formed and consumed before the next face, which
+      // keeps the live state to the element's corners and the four edge
+      // forces.  The faces of side s (neighbours across faces s and s+2)
+      // are (s+3)&3 and s+1, in the reference's order 3, 1, 0, 2.
       const int4 ee = __ldg(F.ielel + iel);
       const int nb[4] = {ee.x, ee.y, ee.z, ee.w};
       const int fcp = __ldg(F.ielfc + iel);
-      // per own face: |du|, 1/max(|du|,zc)-normalised (uhat,vhat), |dx|,
-      // (xhat,yhat) and the inverse of the own normalised gradient w1
-      double lu[4], lx[4], uh[4], vh[4], xh[4], yh[4];
-      double sc[4][2];  // limiter ratios (neighbour across s, across s+2)
-      double edv[4];
+      const double cs2i = F.cs2[iel];
+      const double xc = quarter(x[0] + x[1] + x[2] + x[3]);
+      const double yc = quarter(y[0] + y[1] + y[2] + y[3]);
+      double edx[4], edy[4];
 #pragma unroll
       for (int s = 0; s < 2; s++) {
         const int in1 = nb[s], in2 = nb[s + 2];
         const int f1 = fc_of(fcp, s), f2 = fc_of(fcp, s + 2);
+        // boundary rule (hydro_kn_edgeviscosity.f90:154-183): a ratio across
+        // a boundary face is 1 between two boundary nodes facing an
+        // interior neighbour, 0 otherwise
+        double val1 = 0.0, val2 = 0.0;
+        if (in1 == iel)
+          val1 = (__ldg(F.indtype + n[s]) < 0 && __ldg(F.indtype + n[(s + 1) & 3]) < 0 && in2 != iel)
+                     ? 1.0 : 0.0;
+        if (in2 == iel)
+          val2 = (__ldg(F.indtype + n[s + 2]) < 0 && __ldg(F.indtype + n[(s + 3) & 3]) < 0 &&
+                  in1 != iel) ? 1.0 : 0.0;
 #pragma unroll
         for (int e2 = 0; e2 < 2; e2++) {
           const int is = e2 == 0 ? ((s + 3) & 3) : (s + 1);
-          double w1 = du[is], w2 = dv[is], w3 = dx[is], w4 = dy[is];
+          const int jn = (is + 1) & 3;
+          double w1 = u[jn] - u[is], w2 = v[jn] - v[is];
+          double w3 = x[jn] - x[is], w4 = y[jn] - y[is];
+          const double du = w1, dv = w2;
           double den = SQRT(w1 * w1 + w2 * w2);
-          lu[is] = den;
+          const double lu = den;
           den = DIV(1.0, maxF_nn(den, zc));
-          double uhat = w1 * den, vhat = w2 * den;
+          const double uhat = w1 * den, vhat = w2 * den;
           den = SQRT(w3 * w3 + w4 * w4);
-          lx[is] = den;
+          const double lx = den;
           den = DIV(1.0, maxF_nn(den, zc));
-          double xhat = w3 * den, yhat = w4 * den;
-          uh[is] = uhat;
-          vh[is] = vhat;
-          xh[is] = xhat;
-          yh[is] = yhat;
-          den = w3 * xhat + w4 * yhat;
+          const double xh = w3 * den, yh = w4 * den;
+          den = w3 * xh + w4 * yh;
           w1 = DIV(w1 * uhat + w2 * vhat, signF(maxF_nn(absF(den), zc), den));
           w1 = DIV(1.0, signF(maxF_nn(absF(w1), zc), w1));
           // neighbour faces: edge 1 uses MOD(ielfc,4)+1 / MOD(ielfc+2,4)+1,
           // edge 2 the other pair (hydro_kn_edgeviscosity.f90:117-151)
           const int ins1 = e2 == 0 ? ((f1 + 1) & 3) : ((f1 + 3) & 3);
           const int ins2 = e2 == 0 ? ((f2 + 3) & 3) : ((f2 + 1) & 3);
-          double r1 = 0.0, r2 = 0.0;
-          if (in1 != iel) {  // overwritten by the boundary rule otherwise
+          double r1 = val1, r2 = val2;
+          if (in1 != iel) {
             const int4 m = __ldg(F.ielnd + in1);
             const int mm[4] = {m.x, m.y, m.z, m.w};
             const int a = mm[ins1], b = mm[(ins1 + 1) & 3];
             double ddx = F.ndx[b] - F.ndx[a], ddy = F.ndy[b] - F.ndy[a];
             double ddu = F.ndu[b] - F.ndu[a], ddv = F.ndv[b] - F.ndv[a];
-            double dn = ddx * xhat + ddy * yhat;
+            double dn = ddx * xh + ddy * yh;
             double q = DIV(ddu * uhat + ddv * vhat, signF(maxF_nn(absF(dn), zc), dn));
             r1 = q * w1;
           }
@@ -438,73 +444,46 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
             const int a = mm[ins2], b = mm[(ins2 + 1) & 3];
             double ddx = F.ndx[b] - F.ndx[a], ddy = F.ndy[b] - F.ndy[a];
             double ddu = F.ndu[b] - F.ndu[a], ddv = F.ndv[b] - F.ndv[a];
-            double dn = ddx * xhat + ddy * yhat;
+            double dn = ddx * xh + ddy * yh;
             double q = DIV(ddu * uhat + ddv * vhat, signF(maxF_nn(absF(dn), zc), dn));
             r2 = q * w1;
           }
-          sc[is][0] = r1;
-          sc[is][1] = r2;
-        }
-        // boundary rule (hydro_kn_edgeviscosity.f90:154-183)
-        const int is1 = (s + 3) & 3, is2 = s + 1;
-        if (in1 == iel) {
-          const int ic1 = n[s], ic2 = n[(s + 1) & 3];
-          const double val = (__ldg(F.indtype + ic1) < 0 && __ldg(F.indtype + ic2) < 0 && in2 != iel) ? 1.0 : 0.0;
-          sc[is1][0] = val;
-          sc[is2][0] = val;
-        }
-        if (in2 == iel) {
-          const int ic1 = n[s + 2], ic2 = n[(s + 3) & 3];
-          const double val = (__ldg(F.indtype + ic1) < 0 && __ldg(F.indtype + ic2) < 0 && in1 != iel) ? 1.0 : 0.0;
-          sc[is1][1] = val;
-          sc[is2][1] = val;
-        }
-        // apply limiter (hydro_kn_edgeviscosity.f90:185-214)
-        const double cs2i = F.cs2[iel];
-#pragma unroll
-        for (int e2 = 0; e2 < 2; e2++) {
-          const int is = e2 == 0 ? is1 : is2;
+          // limiter and edge coefficient (hydro_kn_edgeviscosity.f90:185-214)
           const int ins = nb[is];
-          double w1 = C.cvisc1 * SQRT(0.5 * (cs2i + F.cs2[ins]));
-          double w2 = sc[is][0], w3 = sc[is][1];
-          w2 = minF(minF(minF(0.5 * (w2 + w3), 2.0 * w2), 2.0 * w3), 1.0);
+          w1 = C.cvisc1 * SQRT(half(cs2i + F.cs2[ins]));
+          w2 = r1;
+          w3 = r2;
+          w2 = minF(minF(minF(half(w2 + w3), twice(w2)), twice(w3)), 1.0);
           w2 = maxF(0.0, w2);
-          double w4 = lu[is];
-          w3 = 0.5 * (1.0 - w2) * (rho0 + F.rho[ins]) * (w1 + C.cvisc2 * w4);
-          edv[is] = w3;
-          w4 = DIV(2.0 * w4, maxF(rho0, zc));
+          w4 = lu;
+          w3 = half(1.0 - w2) * (rho0 + F.rho[ins]) * (w1 + C.cvisc2 * w4);
+          const double edv = w3;
+          w4 = DIV(twice(w4), maxF(rho0, zc));
           visc = maxF_nn(visc, w3 * w4);  // visc stays +0 or positive
-        }
-      }
-      // hydro_kn_geteviscosity (hydro_kn_edgeviscosity.f90:219-282)
-      const double xc = 0.25 * (x[0] + x[1] + x[2] + x[3]);
-      const double yc = 0.25 * (y[0] + y[1] + y[2] + y[3]);
-      double edx[4], edy[4];
-#pragma unroll
-      for (int f = 0; f < 4; f++) {
-        const int ins = (f + 1) & 3;
-        double w3 = 0.5 * (x[f] + x[ins]);
-        double w6 = 0.5 * (y[f] + y[ins]);
-        double w7 = SQRT((xc - w3) * (xc - w3) + (yc - w6) * (yc - w6));
-        double w8 = lx[f];  // SQRT(w1*w1+w4*w4) of the same face difference
-        double den = DIV(1.0, w7);
-        double xhat = (yc - w6) * den, yhat = (w3 - xc) * den;
-        // w1*(1/w8), w4*(1/w8): equal to the limiter's normalised face
-        // vector whenever w8 > zerocut; otherwise the edge is cut below
-        double q1 = xh[f], q2 = yh[f];
-        double w33 = xhat * q1 + yhat * q2;
-        den = -(signF(1.0, w33) * w7);
-        xhat = xhat * den;
-        yhat = yhat * den;
-        double uhat = du[f], vhat = dv[f];
-        double w5 = lu[f];
-        double w6b = uhat * xhat + vhat * yhat;
-        den = DIV(w6b, maxF_nn(w5, zc));
-        edx[f] = edv[f] * uhat * den;
-        edy[f] = edv[f] * vhat * den;
-        if (le_nn(w5, zc) || geF(zc, w6b) || le_nn(w7, zc) || le_nn(w8, zc)) {
-          edx[f] = 0.0;
-          edy[f] = 0.0;
+          // edge force (hydro_kn_edgeviscosity.f90:219-282)
+          {
+            const double m3 = half(x[is] + x[jn]);
+            const double m6 = half(y[is] + y[jn]);
+            const double w7 = SQRT((xc - m3) * (xc - m3) + (yc - m6) * (yc - m6));
+            const double w8 = lx;  // SQRT(w1*w1+w4*w4) of the same face difference
+            double d = DIV(1.0, w7);
+            double exh = (yc - m6) * d, eyh = (m3 - xc) * d;
+            // w1*(1/w8), w4*(1/w8): the limiter's normalised face vector
+            // whenever w8 > zerocut; otherwise the edge is cut below
+            const double w33 = exh * xh + eyh * yh;
+            d = -(signF(1.0, w33) * w7);
+            exh = exh * d;
+            eyh = eyh * d;
+            const double w5 = lu;
+            const double w6b = du * exh + dv * eyh;
+            d = DIV(w6b, maxF_nn(w5, zc));
+            edx[is] = edv * du * d;
+            edy[is] = edv * dv * d;
+            if (le_nn(w5, zc) || geF(zc, w6b) || le_nn(w7, zc) || le_nn(w8, zc)) {
+              edx[is] = 0.0;
+              edy[is] = 0.0;
+            }
+          }
         }
       }
       qx[0] = edx[0] - edx[3];
@@ -737,7 +716,7 @@ __global__ void __launch_bounds__(BS, BL_FORCE_MINB) k_lag_force(DevFields F, De
       const double cpm = F.cpm[icp];
       const double cpe = energy_update(F.cpe[icp], cpm, zc, hdt, cfx, cfy, cu, cv);
       F.cpe[icp] = cpe;  // the reference does not restore component energy
-      const double cpv = 4.0 * (g.a1 * g.b3 - g.a3 * g.b1) * fr;
+      const double cpv = times4(g.a1 * g.b3 - g.a3 * g.b1) * fr;
       const double cpr = DIV(cpm, cpv);
       double cpp, cpc;
       eos_pc(C, __ldg(F.icpmat + icp), cpr, cpe, cpp, cpc);
@@ -896,7 +875,7 @@ __global__ void __launch_bounds__(BS) k_lag_state(DevFields F, DevCfg C) {
       }
       const double cpm = F.cpm[icp];
       const double cpe = energy_update(F.cpe[icp], cpm, zc, dt, cfx, cfy, cu, cv);
-      const double cpv = 4.0 * (g.a1 * g.b3 - g.a3 * g.b1) * fr;
+      const double cpv = times4(g.a1 * g.b3 - g.a3 * g.b1) * fr;
       const double cpr = DIV(cpm, cpv);
       double cpp, cpc;
       eos_pc(C, __ldg(F.icpmat + icp), cpr, cpe, cpp, cpc);
