@@ -53,6 +53,20 @@
 
 namespace bl {
 
+// Bit patterns through inline PTX moves: the compiler cannot see through
+// them, so it cannot turn the integer tests of the patterns below back into
+// FP64 comparisons, class tests or abs (which would issue on the FP64 pipe).
+__device__ __forceinline__ long long bits64(double x) {
+  long long r;
+  asm("mov.b64 %0, %1;" : "=l"(r) : "d"(x));
+  return r;
+}
+__device__ __forceinline__ double from_bits64(long long b) {
+  double r;
+  asm("mov.b64 %0, %1;" : "=d"(r) : "l"(b));
+  return r;
+}
+
 __device__ __forceinline__ float rcp_approx_f32(float x) {
   float r;
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
@@ -100,6 +114,11 @@ __device__ __forceinline__ uint64_t recip_fixed(uint64_t D) {
   return v;
 }
 
+// The hardware operations for the rare operands, out of line so that none
+// of their FP64 instructions is issued on the common path.
+static __device__ __noinline__ double div_hw(double a, double b) { return a / b; }
+static __device__ __noinline__ double sqrt_hw(double x) { return sqrt(x); }
+
 // Slow-path rounding of a quotient: q <= Q <= q + 8, remainder fixed exactly.
 static __device__ __noinline__ uint64_t ddiv_fix(uint64_t N, uint64_t D, uint64_t q) {
   const uint64_t plo = q * D;
@@ -120,8 +139,8 @@ static __device__ __noinline__ uint64_t ddiv_fix(uint64_t N, uint64_t D, uint64_
 }
 
 __device__ __forceinline__ double ddiv_rn(double a, double b) {
-  const uint64_t ua = (uint64_t)__double_as_longlong(a);
-  const uint64_t ub = (uint64_t)__double_as_longlong(b);
+  const uint64_t ua = (uint64_t)bits64(a);
+  const uint64_t ub = (uint64_t)bits64(b);
   const uint64_t M52 = (1ull << 52) - 1;
   int ea = (int)((ua >> 52) & 0x7FF);
   int eb = (int)((ub >> 52) & 0x7FF);
@@ -131,10 +150,10 @@ __device__ __forceinline__ double ddiv_rn(double a, double b) {
   if ((unsigned)(ea - 1) >= 2046u || (unsigned)(eb - 1) >= 2046u || (unsigned)(ed + 1021) > 2043u) {
     const bool az = (ua << 1) == 0, bz = (ub << 1) == 0;
     // infinities, NaNs and zero divisors: the hardware
-    if (ea == 2047 || eb == 2047 || bz) return a / b;
+    if (ea == 2047 || eb == 2047 || bz) return div_hw(a, b);
     // a zero dividend (common: fluid at rest) gives the zero with the
     // product of the signs
-    if (az) return __longlong_as_double((long long)((ua ^ ub) & 0x8000000000000000ull));
+    if (az) return from_bits64((long long)((ua ^ ub) & 0x8000000000000000ull));
     // subnormal operands (tiny velocity differences ahead of a shock) are
     // normalised, their exponent extended below 1
     if (ea == 0) {
@@ -149,7 +168,7 @@ __device__ __forceinline__ double ddiv_rn(double a, double b) {
     }
     ed = ea - eb;
     // a quotient that may be subnormal or overflow: the hardware
-    if ((unsigned)(ed + 1021) > 2043u) return a / b;
+    if ((unsigned)(ed + 1021) > 2043u) return div_hw(a, b);
   }
   const bool ge = ma >= mb;
   const uint64_t N = ma << (ge ? 10 : 11);
@@ -163,7 +182,7 @@ __device__ __forceinline__ double ddiv_rn(double a, double b) {
   else sig = (q >> 11) + (L > 0x400u ? 1ull : 0ull);
   // the implicit bit of sig carries into the exponent field: (E-1) << 52
   const uint64_t r = (((uint64_t)(E - 1) << 52) + sig) | ((ua ^ ub) & 0x8000000000000000ull);
-  return __longlong_as_double((long long)r);
+  return from_bits64((long long)r);
 }
 
 // Slow-path rounding of a square root: S1 <= S <= S1 + 4.
@@ -187,14 +206,14 @@ static __device__ __noinline__ uint64_t dsqrt_fix(uint64_t Nhi, uint64_t S) {
 }
 
 __device__ __forceinline__ double dsqrt_rn(double x) {
-  const uint64_t ux = (uint64_t)__double_as_longlong(x);
+  const uint64_t ux = (uint64_t)bits64(x);
   const uint64_t M52 = (1ull << 52) - 1;
   const int ex = (int)(ux >> 52);  // with the sign bit: negative x fails the test
   uint64_t M = (ux & M52) | (1ull << 52);
   int u = ex - 1023;
   if ((unsigned)(ex - 1) >= 2046u) {
     if ((ux << 1) == 0) return x;  // sqrt(+-0) = +-0
-    if (ex != 0) return sqrt(x);   // negative, infinite, NaN
+    if (ex != 0) return sqrt_hw(x);  // negative, infinite, NaN
     // positive subnormal: normalise (its square root is a normal number)
     const int s = __clzll((long long)ux) - 11;
     M = ux << s;
@@ -243,7 +262,7 @@ __device__ __forceinline__ double dsqrt_rn(double x) {
   uint64_t sig;
   if ((L + 3u >= 0x400u && L <= 0x400u) || L + 3u > 0x7FFu) sig = dsqrt_fix(Nhi, S);
   else sig = (S >> 11) + (L > 0x400u ? 1ull : 0ull);
-  return __longlong_as_double((long long)(((uint64_t)(E - 1) << 52) + sig));
+  return from_bits64((long long)(((uint64_t)(E - 1) << 52) + sig));
 }
 
 // ------------------------------------------------------------ powers of two
@@ -257,10 +276,10 @@ __device__ __forceinline__ double dsqrt_rn(double x) {
 static __device__ __noinline__ double ldexp_slow(double x, double s) { return x * s; }
 template <int K>
 __device__ __forceinline__ double ldexpF(double x) {
-  const long long b = __double_as_longlong(x);
+  const long long b = bits64(x);
   const int e = (int)((b >> 52) & 0x7FF);
   if ((unsigned)(e - 1) < 2046u && (unsigned)(e + K - 1) < 2046u)
-    return __longlong_as_double(b + (long long)((unsigned long long)(long long)K << 52));
+    return from_bits64(b + (long long)((unsigned long long)(long long)K << 52));
   if (((unsigned long long)b << 1) == 0) return x;
   return ldexp_slow(x, K >= 0 ? (double)(1 << (K >= 0 ? K : 0)) : 1.0 / (double)(1 << (K < 0 ? -K : 0)));
 }
@@ -275,11 +294,10 @@ __device__ __forceinline__ double times4(double x) { return ldexpF<2>(x); }
 // word (integer pipe); an FP64 abs or negate that the compiler cannot fold
 // into a neighbouring instruction would otherwise occupy an FP64 issue slot.
 __device__ __forceinline__ double absF(double x) {
-  return __hiloint2double(__double2hiint(x) & 0x7FFFFFFF, __double2loint(x));
+  return from_bits64(bits64(x) & 0x7FFFFFFFFFFFFFFFll);
 }
 __device__ __forceinline__ double signF(double a, double b) {
-  return __hiloint2double((__double2hiint(a) & 0x7FFFFFFF) | (__double2hiint(b) & (int)0x80000000),
-                          __double2loint(a));
+  return from_bits64((bits64(a) & 0x7FFFFFFFFFFFFFFFll) | (bits64(b) & (long long)0x8000000000000000ull));
 }
 
 // ------------------------------------------------------------ comparisons
@@ -287,11 +305,11 @@ __device__ __forceinline__ double signF(double a, double b) {
 // Order key: monotone in the value over non-NaN doubles, with -0 and +0 both
 // mapped to 0 (for negative x the key is minus the magnitude bits).
 __device__ __forceinline__ long long okey(double x) {
-  const long long i = __double_as_longlong(x);
+  const long long i = bits64(x);
   return i < 0 ? (LLONG_MIN - i) : i;
 }
 __device__ __forceinline__ bool nanF(double x) {
-  return ((unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull) >
+  return ((unsigned long long)bits64(x) & 0x7FFFFFFFFFFFFFFFull) >
          0x7FF0000000000000ull;
 }
 // IEEE a > b, a >= b (false when either is NaN)
@@ -305,12 +323,12 @@ __device__ __forceinline__ bool geF(double a, double b) {
 // for any a: a sign-bit-set a is then never above b, and the plain integer
 // order of sign-clear patterns is the value order with NaNs at the top.
 __device__ __forceinline__ bool gt_nn(double a, double b) {
-  const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+  const long long ia = bits64(a), ib = bits64(b);
   return ia > ib && ia <= 0x7FF0000000000000ll;
 }
 // IEEE a <= b when a's sign bit is clear, for any b
 __device__ __forceinline__ bool le_nn(double a, double b) {
-  const long long ia = __double_as_longlong(a);
+  const long long ia = bits64(a);
   return ia <= okey(b) && ia <= 0x7FF0000000000000ll && !nanF(b);
 }
 

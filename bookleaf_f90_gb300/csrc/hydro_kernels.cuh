@@ -343,7 +343,7 @@ __device__ __forceinline__ void cfl_min(double& v, int& i, double ov, int oi) {
 // DIV candidates are TINY or values that exceeded it: positive, never NaN,
 // so their bit patterns order as integers
 __device__ __forceinline__ void div_max(double& v, int& i, double ov, int oi) {
-  const long long io = __double_as_longlong(ov), iv = __double_as_longlong(v);
+  const long long io = bits64(ov), iv = bits64(v);
   if (io > iv || (io == iv && oi >= 0 && (i < 0 || oi < i))) { v = ov; i = oi; }
 }
 
