@@ -293,6 +293,9 @@ __device__ __forceinline__ double times4(double x) { return ldexpF<2>(x); }
 // |x| and Fortran SIGN(|a|, b) as operations on the sign bit of the high
 // word (integer pipe); an FP64 abs or negate that the compiler cannot fold
 // into a neighbouring instruction would otherwise occupy an FP64 issue slot.
+__device__ __forceinline__ double negF(double x) {
+  return from_bits64(bits64(x) ^ (long long)0x8000000000000000ull);
+}
 __device__ __forceinline__ double absF(double x) {
   return from_bits64(bits64(x) & 0x7FFFFFFFFFFFFFFFll);
 }

@@ -34,6 +34,22 @@
 // Every FP64 division and square root of the path goes through the
 // integer-pipe versions, which return the IEEE results bit for bit
 // (bl_fp64.cuh).
+// The divides and square roots run out of line: one body per kernel instead
+// of ~60 inlined copies of ~100 instructions, which overflowed the
+// instruction cache (k_getdt stalled on instruction fetch); measured on the
+// GB300 over the whole Sedov 512x512 run: 556.1M zone-cycles/s against
+// 514.6M inlined.
+#ifndef BL_DIV_CALL
+#define BL_DIV_CALL 1
+#endif
+#if BL_DIV_CALL
+namespace bl {
+static __device__ __noinline__ double ddiv_call(double a, double b) { return ddiv_rn(a, b); }
+static __device__ __noinline__ double dsqrt_call(double x) { return dsqrt_rn(x); }
+}  // namespace bl
+#define DIV(a, b) ::bl::ddiv_call((a), (b))
+#define SQRT(a) ::bl::dsqrt_call(a)
+#endif
 #ifndef DIV
 #define DIV(a, b) ::bl::ddiv_rn((a), (b))
 #endif
@@ -228,9 +244,43 @@ __device__ __forceinline__ void force_pq(double p, double a1, double a3, double 
   fy[3] = fy[3] + qy.w;
 }
 
-// hydro_kn_getforceSP (hydro_kn_getforce.f90:109-188)
+#if BL_FAST_ALGEBRA
+// Sub-zone coefficients of the fast build from the element's iso-parametric
+// ones.  With the corners written as s - a1 + a2 - a3, s + a1 - a2 - a3,
+// s + a1 + a2 + a3, s - a1 - a2 + a3 (s the centroid), the sub-quad of
+// corner j (the corner, the edge midpoint after it, the centroid, the edge
+// midpoint before it) has
+//   w3 = P/4, R/4, -S/4, -Q/4 and w4 = Q/4, -P/4, -R/4, S/4 (j = 0..3)
+// with P = 2a1 - a2, Q = 2a3 - a2, R = 2a3 + a2, S = 2a1 + a2: exact in real
+// arithmetic, rounded once here instead of through the midpoints and the
+// centroid.
+__device__ __forceinline__ void sp_coeffs(double a1, double a2, double a3, double* w3,
+                                          double* w4) {
+  const double P = twice(a1) - a2, Q = twice(a3) - a2, R = twice(a3) + a2, S = twice(a1) + a2;
+  w3[0] = quarter(P);
+  w3[1] = quarter(R);
+  w3[2] = negF(quarter(S));
+  w3[3] = negF(quarter(Q));
+  w4[0] = quarter(Q);
+  w4[1] = negF(quarter(P));
+  w4[2] = negF(quarter(R));
+  w4[3] = quarter(S);
+}
+#endif
+
+// hydro_kn_getforceSP (hydro_kn_getforce.f90:109-188).  iso holds the
+// element's a1,a2,a3,b1,b2,b3 at the same vertices (used by the fast
+// build only).
 __device__ void force_sp(double w1, double rho, double cs2, const double* cx, const double* cy,
-                         const d4& spm, double* fx, double* fy) {
+                         const double* iso, const d4& spm, double* fx, double* fy) {
+#if BL_FAST_ALGEBRA
+  (void)cx;
+  (void)cy;
+  double W3[4], W4[4], W5[4], W6[4];
+  sp_coeffs(iso[0], iso[1], iso[2], W3, W4);
+  sp_coeffs(iso[3], iso[4], iso[5], W5, W6);
+#else
+  (void)iso;
   double x3 = quarter(cx[0] + cx[1] + cx[2] + cx[3]);
   double y3 = quarter(cy[0] + cy[1] + cy[2] + cy[3]);
   // edge midpoints: x2 of corner j and x4 of corner j+1 are the same sum
@@ -241,9 +291,13 @@ __device__ void force_sp(double w1, double rho, double cs2, const double* cx, co
     mx[j] = half(cx[j] + cx[(j + 1) & 3]);
     my[j] = half(cy[j] + cy[(j + 1) & 3]);
   }
+#endif
   double lfx[4][4], lfy[4][4];
 #pragma unroll
   for (int j1 = 0; j1 < 4; j1++) {
+#if BL_FAST_ALGEBRA
+    const double w3 = W3[j1], w4 = W4[j1], w5 = W5[j1], w6 = W6[j1];
+#else
     double x1 = cx[j1], y1 = cy[j1];
     double x2 = mx[j1], y2 = my[j1];
     double x4 = mx[(j1 + 3) & 3], y4 = my[(j1 + 3) & 3];
@@ -251,6 +305,7 @@ __device__ void force_sp(double w1, double rho, double cs2, const double* cx, co
     double w4 = quarter(-x1 - x2 + x3 + x4);
     double w5 = quarter(-y1 + y2 + y3 - y4);
     double w6 = quarter(-y1 - y2 + y3 + y4);
+#endif
     double w2 = times4(w3 * w6 - w4 * w5);
     w2 = DIV(c4(spm, j1), w2);
     w2 = w2 - rho;
@@ -678,8 +733,14 @@ __global__ void __launch_bounds__(BS, BL_FORCE_MINB) k_lag_force(DevFields F, De
   double fx[4], fy[4];
   // ---- predictor force at t^n (hydro_dr_getforce, zcorrector false)
   force_pq(F.p[iel], F.a1[iel], F.a3[iel], F.b1[iel], F.b3[iel], qx, qy, fx, fy);
-  if (C.zsp)
-    force_sp(__ldg(C.pmeritreg + ireg), F.rho[iel], F.cs2v[iel], x, y, F.spmass[iel], fx, fy);
+  if (C.zsp) {
+#if BL_FAST_ALGEBRA
+    const double iso[6] = {F.a1[iel], F.a2[iel], F.a3[iel], F.b1[iel], F.b2[iel], F.b3[iel]};
+#else
+    const double* iso = nullptr;
+#endif
+    force_sp(__ldg(C.pmeritreg + ireg), F.rho[iel], F.cs2v[iel], x, y, iso, F.spmass[iel], fx, fy);
+  }
   // ---- half-step vertices (geometry_kn_getvertex with 0.5*dt)
   double xh[4], yh[4];
 #pragma unroll
@@ -739,8 +800,10 @@ __global__ void __launch_bounds__(BS, BL_FORCE_MINB) k_lag_force(DevFields F, De
   } else {
     // ---- corrector force at the half step (zcorrector true)
     force_pq(ph, g.a1, g.a3, g.b1, g.b3, qx, qy, fx, fy);
-    if (C.zsp)
-      force_sp(__ldg(C.pmeritreg + ireg), rho, cs2h, xh, yh, F.spmass[iel], fx, fy);
+    if (C.zsp) {
+      const double iso[6] = {g.a1, g.a2, g.a3, g.b1, g.b2, g.b3};
+      force_sp(__ldg(C.pmeritreg + ireg), rho, cs2h, xh, yh, iso, F.spmass[iel], fx, fy);
+    }
     if (C.zhg) force_hg(__ldg(C.kappareg + ireg), rho, g.vol, S->rdt, u, v, fx, fy);
   }
   F.cnfx[iel] = make_d4(fx[0], fx[1], fx[2], fx[3]);
