@@ -49,8 +49,8 @@ B_GETDT = 164
 # (DFMA+DMUL+DADD+DSETP) it executes per zone, which with the FMA rate
 # measured live below place k_getdt against the FP64 issue roof that binds
 # it, and its DRAM traffic per launch (dram__bytes_read + _write).
-FP64_PER_ZONE_GETDT = 369
-TRAFFIC_GETDT_BYTES = 35.0e6
+FP64_PER_ZONE_GETDT = 290
+TRAFFIC_GETDT_BYTES = 35.3e6
 
 
 def workload_deck(name, size):

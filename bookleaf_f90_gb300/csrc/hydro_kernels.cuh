@@ -443,8 +443,16 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
       const int nb[4] = {ee.x, ee.y, ee.z, ee.w};
       const int fcp = __ldg(F.ielfc + iel);
       const double cs2i = F.cs2[iel];
+#if BL_FAST_ALGEBRA
+      // fast build: the vector from an edge's midpoint to the centroid is
+      // (a3,b3), (-a1,-b1), (-a3,-b3), (a1,b1) for faces 0..3 (corners
+      // written as s -+ a1 +- a2 -+ a3, exact in real arithmetic), from the
+      // element's iso-parametric coefficients at these vertices
+      const double ga1 = F.a1[iel], ga3 = F.a3[iel], gb1 = F.b1[iel], gb3 = F.b3[iel];
+#else
       const double xc = quarter(x[0] + x[1] + x[2] + x[3]);
       const double yc = quarter(y[0] + y[1] + y[2] + y[3]);
+#endif
       double edx[4], edy[4];
 #pragma unroll
       for (int s = 0; s < 2; s++) {
@@ -516,6 +524,31 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
           w4 = DIV(twice(w4), maxF(rho0, zc));
           visc = maxF_nn(visc, w3 * w4);  // visc stays +0 or positive
           // edge force (hydro_kn_edgeviscosity.f90:219-282)
+#if BL_FAST_ALGEBRA
+          {
+            // the reference normalises the midpoint-to-centroid vector c,
+            // orients it by the sign of its product with the face vector and
+            // scales it back by |c|: (exh, eyh) = -+(cy, -cx), the sign bit
+            // of w33 = cy*xh - cx*yh choosing; |c| only enters the cut test
+            const double cx = is == 0 ? ga3 : (is == 1 ? negF(ga1) : (is == 2 ? negF(ga3) : ga1));
+            const double cy = is == 0 ? gb3 : (is == 1 ? negF(gb1) : (is == 2 ? negF(gb3) : gb1));
+            const double w33 = cy * xh - cx * yh;
+            const long long sb = bits64(w33) & (long long)0x8000000000000000ull;
+            const double exh = from_bits64(bits64(cy) ^ (long long)0x8000000000000000ull ^ sb);
+            const double eyh = from_bits64(bits64(cx) ^ sb);
+            const double w7sq = cx * cx + cy * cy;
+            const double w8 = lx;
+            const double w5 = lu;
+            const double w6b = du * exh + dv * eyh;
+            const double d = DIV(w6b, maxF_nn(w5, zc));
+            edx[is] = edv * du * d;
+            edy[is] = edv * dv * d;
+            if (le_nn(w5, zc) || geF(zc, w6b) || le_nn(w7sq, zc * zc) || le_nn(w8, zc)) {
+              edx[is] = 0.0;
+              edy[is] = 0.0;
+            }
+          }
+#else
           {
             const double m3 = half(x[is] + x[jn]);
             const double m6 = half(y[is] + y[jn]);
@@ -539,6 +572,7 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
               edy[is] = 0.0;
             }
           }
+#endif
         }
       }
       qx[0] = edx[0] - edx[3];
