@@ -187,6 +187,42 @@ __device__ __forceinline__ double min_dln(const double* x, const double* y, doub
   return m;
 }
 
+#if BL_FAST_ALGEBRA
+// Fast build: the same squared lengths from the element's iso-parametric
+// coefficients.  For side k the opposite edge (corners k+2 -> k+3) is
+// 2*(dx,dy) with (dx,dy) = (a1+a2, b1+b2), (a2-a3, b2-b3), (a1-a2, b1-b2),
+// (a2+a3, b2+b3), and its cross product with the vector to the midpoint of
+// corners k,k+1 is 4*(dx*q - dy*p) with (p,q) = (a3,b3), (a1,b1), (a3,b3),
+// (a1,b1); so the reference's distpl/denom is 4 X^2 / Y with X = dx*q -
+// dy*p and Y = dx^2 + dy^2 (exact in real arithmetic), and its denominator
+// is 4 Y.  A degenerate opposite edge (4 Y < zcut) takes the corner form.
+__device__ __forceinline__ double min_dln_iso(const double* x, const double* y, double zcut,
+                                              double a1, double a2, double a3, double b1,
+                                              double b2, double b3) {
+  const double dxs[4] = {a1 + a2, a2 - a3, a1 - a2, a2 + a3};
+  const double dys[4] = {b1 + b2, b2 - b3, b1 - b2, b2 + b3};
+  double r[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const double dx = dxs[k], dy = dys[k];
+    const double p = (k & 1) ? a1 : a3, q = (k & 1) ? b1 : b3;
+    const double Y = dx * dx + dy * dy;
+    if (gt_nn(zcut, times4(Y))) {
+      const int a = k, b = (k + 1) & 3, c = (k + 2) & 3;
+      r[k] = g_distpp(x[a], y[a], x[b], y[b], x[c], y[c]);
+    } else {
+      const double X = dx * q - dy * p;
+      r[k] = DIV(times4(X * X), Y);
+    }
+  }
+  double m = r[0];
+  m = minF_nn(m, r[1]);
+  m = minF_nn(m, r[2]);
+  m = minF_nn(m, r[3]);
+  return m;
+}
+#endif
+
 // MINVAL(geometry_kn_dlm(...)) (geometry_kn_length.f90:30-56)
 __device__ __forceinline__ double min_dlm(const double* x, const double* y) {
   double x1 = x[0] + x[1], x2 = x[2] + x[3], y1 = y[0] + y[1], y2 = y[2] + y[3];
@@ -605,7 +641,14 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
     if (__ldg(C.zdtnotreg + ireg)) {
       r11 = DBL_MAX;
     } else {
+#if BL_FAST_ALGEBRA
+      double w1 = __ldg(C.zmidlength + ireg)
+                      ? min_dlm(x, y)
+                      : min_dln_iso(x, y, C.zcut, F.a1[iel], F.a2[iel], F.a3[iel], F.b1[iel],
+                                    F.b2[iel], F.b3[iel]);
+#else
       double w1 = __ldg(C.zmidlength + ireg) ? min_dlm(x, y) : min_dln(x, y, C.zcut);
+#endif
       r11 = DIV(w1, cs2v);
     }
     cflv = r11;
