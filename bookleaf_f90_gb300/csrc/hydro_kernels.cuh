@@ -128,8 +128,42 @@ __device__ __forceinline__ void eos_pc(const DevCfg& C, int mat, double rho, dou
 // geometry_kn_getiso + getvolume (geometry_kn_volume.f90:30-79)
 struct Iso {
   double a1, a2, a3, b1, b2, b3, w0, w1, w2, w3, vol;
+  // fast build: a1*b3 - a3*b1 and the two skew products' sum and
+  // difference, T1 + T3 and T3 - T1 with T1 = a1*b2 - a2*b1 and
+  // T3 = a3*b2 - a2*b3 (shared with the sub-zonal pressure force)
+  double cross, ts, td;
 };
 
+#if BL_FAST_ALGEBRA
+// Fast build: the same quantities with fewer roundings.  a1 and a3 share
+// the diagonal differences (x2-x0) +- (x1-x3).  Expanding the reference's
+// corner weights, (3b3 -+ b2)(3a1 -+ a2) - (3a3 -+ a2)(3b1 -+ b2) over 9,
+// gives cross + (T3 - T1)/3, cross + (T1 + T3)/3, cross - (T3 - T1)/3,
+// cross - (T1 + T3)/3 for corners 0..3 (exact in real arithmetic).
+__device__ __forceinline__ Iso getiso(const double* x, const double* y) {
+  Iso g;
+  const double ux = x[2] - x[0], vx = x[1] - x[3];
+  const double uy = y[2] - y[0], vy = y[1] - y[3];
+  g.a1 = quarter(ux + vx);
+  g.a3 = quarter(ux - vx);
+  g.a2 = quarter((x[0] + x[2]) - (x[1] + x[3]));
+  g.b1 = quarter(uy + vy);
+  g.b3 = quarter(uy - vy);
+  g.b2 = quarter((y[0] + y[2]) - (y[1] + y[3]));
+  g.cross = g.a1 * g.b3 - g.a3 * g.b1;
+  const double t1 = g.a1 * g.b2 - g.a2 * g.b1;
+  const double t3 = g.a3 * g.b2 - g.a2 * g.b3;
+  g.ts = t1 + t3;
+  g.td = t3 - t1;
+  const double o3 = 1.0 / 3.0;
+  g.w0 = fma(g.td, o3, g.cross);
+  g.w1 = fma(g.ts, o3, g.cross);
+  g.w2 = fma(-g.td, o3, g.cross);
+  g.w3 = fma(-g.ts, o3, g.cross);
+  g.vol = times4(g.cross);
+  return g;
+}
+#else
 __device__ __forceinline__ Iso getiso(const double* x, const double* y) {
   Iso g;
   g.a1 = quarter(-x[0] + x[1] + x[2] - x[3]);
@@ -148,8 +182,10 @@ __device__ __forceinline__ Iso getiso(const double* x, const double* y) {
   g.w2 = o9 * (B3p * A1p - A3p * B1p);
   g.w3 = o9 * (B3m * A1p - A3m * B1p);
   g.vol = times4(g.a1 * g.b3 - g.a3 * g.b1);
+  g.cross = g.ts = g.td = 0.0;
   return g;
 }
+#endif
 
 // geometry_kn_length (geometry_kn_length.f90:99-139)
 __device__ __forceinline__ double g_denom(double x1, double y1, double x2, double y2) {
@@ -249,17 +285,18 @@ __device__ __forceinline__ void force_pq(double p, double a1, double a3, double 
                                          const d4& qx, const d4& qy, double* fx,
                                          double* fy) {
 #if BL_FAST_ALGEBRA
-  // opposite corners carry opposite coefficients: b3 - b1 = -(-b3 + b1)
-  // exactly, up to the sign of a zero
-  const double cb0 = -b3 + b1, cb1 = b3 + b1, ca0 = a3 - a1, ca1 = -a3 - a1;
-  fx[0] = p * cb0;
-  fx[1] = p * cb1;
-  fx[2] = p * -cb0;
-  fx[3] = p * -cb1;
-  fy[0] = p * ca0;
-  fy[1] = p * ca1;
-  fy[2] = p * -ca0;
-  fy[3] = p * -ca1;
+  // opposite corners carry opposite coefficients: b3 - b1 = -(b1 - b3)
+  // exactly, up to the sign of a zero.  The four sums are the ones the
+  // sub-zonal pressure force uses too.
+  const double db = b1 - b3, sb = b1 + b3, da = a1 - a3, sa = a1 + a3;
+  fx[0] = fma(p, db, qx.x);
+  fx[1] = fma(p, sb, qx.y);
+  fx[2] = fma(-p, db, qx.z);
+  fx[3] = fma(-p, sb, qx.w);
+  fy[0] = fma(-p, da, qy.x);
+  fy[1] = fma(-p, sa, qy.y);
+  fy[2] = fma(p, da, qy.z);
+  fy[3] = fma(p, sa, qy.w);
 #else
   fx[0] = p * (-b3 + b1);
   fx[1] = p * (b3 + b1);
@@ -269,7 +306,6 @@ __device__ __forceinline__ void force_pq(double p, double a1, double a3, double 
   fy[1] = p * (-a3 - a1);
   fy[2] = p * (-a3 + a1);
   fy[3] = p * (a3 + a1);
-#endif
   fx[0] = fx[0] + qx.x;
   fy[0] = fy[0] + qy.x;
   fx[1] = fx[1] + qx.y;
@@ -278,45 +314,69 @@ __device__ __forceinline__ void force_pq(double p, double a1, double a3, double 
   fy[2] = fy[2] + qy.z;
   fx[3] = fx[3] + qx.w;
   fy[3] = fy[3] + qy.w;
-}
-
-#if BL_FAST_ALGEBRA
-// Sub-zone coefficients of the fast build from the element's iso-parametric
-// ones.  With the corners written as s - a1 + a2 - a3, s + a1 - a2 - a3,
-// s + a1 + a2 + a3, s - a1 - a2 + a3 (s the centroid), the sub-quad of
-// corner j (the corner, the edge midpoint after it, the centroid, the edge
-// midpoint before it) has
-//   w3 = P/4, R/4, -S/4, -Q/4 and w4 = Q/4, -P/4, -R/4, S/4 (j = 0..3)
-// with P = 2a1 - a2, Q = 2a3 - a2, R = 2a3 + a2, S = 2a1 + a2: exact in real
-// arithmetic, rounded once here instead of through the midpoints and the
-// centroid.
-__device__ __forceinline__ void sp_coeffs(double a1, double a2, double a3, double* w3,
-                                          double* w4) {
-  const double P = twice(a1) - a2, Q = twice(a3) - a2, R = twice(a3) + a2, S = twice(a1) + a2;
-  w3[0] = quarter(P);
-  w3[1] = quarter(R);
-  w3[2] = negF(quarter(S));
-  w3[3] = negF(quarter(Q));
-  w4[0] = quarter(Q);
-  w4[1] = negF(quarter(P));
-  w4[2] = negF(quarter(R));
-  w4[3] = quarter(S);
-}
 #endif
+}
 
-// hydro_kn_getforceSP (hydro_kn_getforce.f90:109-188).  iso holds the
-// element's a1,a2,a3,b1,b2,b3 at the same vertices (used by the fast
-// build only).
-__device__ void force_sp(double w1, double rho, double cs2, const double* cx, const double* cy,
-                         const double* iso, const d4& spm, double* fx, double* fy) {
 #if BL_FAST_ALGEBRA
-  (void)cx;
-  (void)cy;
-  double W3[4], W4[4], W5[4], W6[4];
-  sp_coeffs(iso[0], iso[1], iso[2], W3, W4);
-  sp_coeffs(iso[3], iso[4], iso[5], W5, W6);
+// Fast build: hydro_kn_getforceSP (hydro_kn_getforce.f90:109-188) from the
+// element's iso-parametric coefficients.  With the corners written as
+// s - a1 + a2 - a3, s + a1 - a2 - a3, s + a1 + a2 + a3, s - a1 - a2 + a3
+// (s the centroid), the sub-quad of corner j (the corner, the edge midpoint
+// after it, the centroid, the edge midpoint before it) has the x
+// coefficients (w3, w4) = (P, Q), (R, -P), (-S, -R), (-Q, S), all over 4,
+// with P = 2a1 - a2, Q = 2a3 - a2, R = 2a3 + a2, S = 2a1 + a2, and the y
+// coefficients (w5, w6) likewise from the b's.  Expanding (all exact in
+// real arithmetic):
+// - the sub-volumes 4(w3 w6 - w4 w5) are V_j = cross + td/2, cross + ts/2,
+//   cross - td/2, cross - ts/2 (cross = a1 b3 - a3 b1, ts = T1 + T3,
+//   td = T3 - T1, T1 = a1 b2 - a2 b1, T3 = a3 b2 - a2 b3);
+// - with p_j = cs2 (spmass_j / V_j - rho), the reference's corner x forces
+//   lfx(j,1) = p_j (w5 - w6) and lfx(j,2) = p_j (w5 + w6) are p_j c_j / 2
+//   and p_j C_j / 2 with c = (db, sb, -db, -sb) and
+//   C = (sb - b2, b2 - db, -(sb + b2), db + b2), db = b1 - b3, sb = b1 + b3;
+//   lfx(j,3) and lfx(j,4) are their negatives;
+// - in the reference's gather of the sub-quad forces to the corners the
+//   midpoint terms of adjacent sub-quads cancel pairwise, leaving, with
+//   M_j = p_j C_j and G = db (p0 - p2) + sb (p1 - p3),
+//   fx0 += w1/8 (4 p0 db + 2 (M3 - M1) - G),
+//   fx1 += w1/8 (4 p1 sb + 2 (M0 - M2) - G),
+//   fx2 -= w1/8 (4 p2 db + 2 (M3 - M1) + G),
+//   fx3 -= w1/8 (4 p3 sb + 2 (M0 - M2) + G);
+// - the y forces are the same with the a's in place of the b's and the
+//   sign of w1 reversed.
+__device__ __forceinline__ void sp_direction(double k, const double* p, double e02, double e13,
+                                             double c1, double c2, double c3, double* f) {
+  const double dd = c1 - c3, ss = c1 + c3;
+  const double m0 = p[0] * (ss - c2), m1 = p[1] * (c2 - dd);
+  const double m2 = -(p[2] * (ss + c2)), m3 = p[3] * (dd + c2);
+  const double d13 = twice(m3 - m1), d02 = twice(m0 - m2);
+  const double g = fma(dd, e02, ss * e13);
+  const double d4 = times4(dd), s4 = times4(ss);
+  f[0] = fma(k, fma(p[0], d4, d13) - g, f[0]);
+  f[1] = fma(k, fma(p[1], s4, d02) - g, f[1]);
+  f[2] = fma(-k, fma(p[2], d4, d13) + g, f[2]);
+  f[3] = fma(-k, fma(p[3], s4, d02) + g, f[3]);
+}
+
+__device__ __forceinline__ void force_sp_iso(double w1, double rho, double cs2, double cross,
+                                             double ts, double td, double a1, double a2,
+                                             double a3, double b1, double b2, double b3,
+                                             const d4& spm, double* fx, double* fy) {
+  const double V[4] = {fma(td, 0.5, cross), fma(ts, 0.5, cross), fma(-td, 0.5, cross),
+                       fma(-ts, 0.5, cross)};
+  const double cr = cs2 * rho;
+  double p[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) p[j] = fma(cs2, DIV(c4(spm, j), V[j]), -cr);
+  const double e02 = p[0] - p[2], e13 = p[1] - p[3];
+  const double k = ldexpF<-3>(w1);
+  sp_direction(k, p, e02, e13, b1, b2, b3, fx);
+  sp_direction(-k, p, e02, e13, a1, a2, a3, fy);
+}
 #else
-  (void)iso;
+// hydro_kn_getforceSP (hydro_kn_getforce.f90:109-188)
+__device__ void force_sp(double w1, double rho, double cs2, const double* cx, const double* cy,
+                         const d4& spm, double* fx, double* fy) {
   double x3 = quarter(cx[0] + cx[1] + cx[2] + cx[3]);
   double y3 = quarter(cy[0] + cy[1] + cy[2] + cy[3]);
   // edge midpoints: x2 of corner j and x4 of corner j+1 are the same sum
@@ -327,13 +387,9 @@ __device__ void force_sp(double w1, double rho, double cs2, const double* cx, co
     mx[j] = half(cx[j] + cx[(j + 1) & 3]);
     my[j] = half(cy[j] + cy[(j + 1) & 3]);
   }
-#endif
   double lfx[4][4], lfy[4][4];
 #pragma unroll
   for (int j1 = 0; j1 < 4; j1++) {
-#if BL_FAST_ALGEBRA
-    const double w3 = W3[j1], w4 = W4[j1], w5 = W5[j1], w6 = W6[j1];
-#else
     double x1 = cx[j1], y1 = cy[j1];
     double x2 = mx[j1], y2 = my[j1];
     double x4 = mx[(j1 + 3) & 3], y4 = my[(j1 + 3) & 3];
@@ -341,23 +397,10 @@ __device__ void force_sp(double w1, double rho, double cs2, const double* cx, co
     double w4 = quarter(-x1 - x2 + x3 + x4);
     double w5 = quarter(-y1 + y2 + y3 - y4);
     double w6 = quarter(-y1 - y2 + y3 + y4);
-#endif
     double w2 = times4(w3 * w6 - w4 * w5);
     w2 = DIV(c4(spm, j1), w2);
     w2 = w2 - rho;
     w2 = cs2 * w2;
-#if BL_FAST_ALGEBRA
-    // -w5 + w6 = -(w5 - w6) and -w5 - w6 = -(w5 + w6) exactly, up to the
-    // sign of a zero: half the products
-    lfx[j1][0] = w2 * (w5 - w6);
-    lfx[j1][1] = w2 * (w5 + w6);
-    lfx[j1][2] = -lfx[j1][0];
-    lfx[j1][3] = -lfx[j1][1];
-    lfy[j1][0] = w2 * (-w3 + w4);
-    lfy[j1][1] = w2 * (-w3 - w4);
-    lfy[j1][2] = -lfy[j1][0];
-    lfy[j1][3] = -lfy[j1][1];
-#else
     lfx[j1][0] = w2 * (w5 - w6);
     lfx[j1][1] = w2 * (w5 + w6);
     lfx[j1][2] = w2 * (-w5 + w6);
@@ -366,7 +409,6 @@ __device__ void force_sp(double w1, double rho, double cs2, const double* cx, co
     lfy[j1][1] = w2 * (-w3 - w4);
     lfy[j1][2] = w2 * (w3 - w4);
     lfy[j1][3] = w2 * (w3 + w4);
-#endif
   }
   double w2 = half(lfx[0][3] + lfx[3][1]);
   double w3 = half(lfx[0][1] + lfx[1][3]);
@@ -387,6 +429,7 @@ __device__ void force_sp(double w1, double rho, double cs2, const double* cx, co
   fy[2] = fy[2] + w1 * (lfy[2][0] + w4 + w5 + w6);
   fy[3] = fy[3] + w1 * (lfy[3][0] + w2 + w5 + w6);
 }
+#endif
 
 // hydro_kn_getforceHG (hydro_kn_getforce.f90:73-107)
 __device__ __forceinline__ void force_hg(double kappa, double rho, double area, double rdt,
@@ -809,14 +852,18 @@ __global__ void __launch_bounds__(BS, BL_FORCE_MINB) k_lag_force(DevFields F, De
   const int imx = F.elmx ? F.elmx[iel] : -1;
   double fx[4], fy[4];
   // ---- predictor force at t^n (hydro_dr_getforce, zcorrector false)
-  force_pq(F.p[iel], F.a1[iel], F.a3[iel], F.b1[iel], F.b3[iel], qx, qy, fx, fy);
+  const double a1 = F.a1[iel], a3 = F.a3[iel], b1 = F.b1[iel], b3 = F.b3[iel];
+  force_pq(F.p[iel], a1, a3, b1, b3, qx, qy, fx, fy);
   if (C.zsp) {
 #if BL_FAST_ALGEBRA
-    const double iso[6] = {F.a1[iel], F.a2[iel], F.a3[iel], F.b1[iel], F.b2[iel], F.b3[iel]};
+    const double a2 = F.a2[iel], b2 = F.b2[iel];
+    const double cross = a1 * b3 - a3 * b1;
+    const double t1 = a1 * b2 - a2 * b1, t3 = a3 * b2 - a2 * b3;
+    force_sp_iso(__ldg(C.pmeritreg + ireg), F.rho[iel], F.cs2v[iel], cross, t1 + t3, t3 - t1, a1,
+                 a2, a3, b1, b2, b3, F.spmass[iel], fx, fy);
 #else
-    const double* iso = nullptr;
+    force_sp(__ldg(C.pmeritreg + ireg), F.rho[iel], F.cs2v[iel], x, y, F.spmass[iel], fx, fy);
 #endif
-    force_sp(__ldg(C.pmeritreg + ireg), F.rho[iel], F.cs2v[iel], x, y, iso, F.spmass[iel], fx, fy);
   }
   // ---- half-step vertices (geometry_kn_getvertex with 0.5*dt)
   double xh[4], yh[4];
@@ -842,7 +889,7 @@ __global__ void __launch_bounds__(BS, BL_FORCE_MINB) k_lag_force(DevFields F, De
       const double fr = F.frvol[icp];
       // predictor component force with the t^n component state
       double cfx[4], cfy[4];
-      force_pq(F.cpp[icp], F.a1[iel], F.a3[iel], F.b1[iel], F.b3[iel], F.cpviscx[icp],
+      force_pq(F.cpp[icp], a1, a3, b1, b3, F.cpviscx[icp],
                F.cpviscy[icp], cfx, cfy);
       // component energy with cpu = frvolume*cnu (utils_kn_mxgathercnav)
       double cu[4], cv[4];
@@ -878,8 +925,12 @@ __global__ void __launch_bounds__(BS, BL_FORCE_MINB) k_lag_force(DevFields F, De
     // ---- corrector force at the half step (zcorrector true)
     force_pq(ph, g.a1, g.a3, g.b1, g.b3, qx, qy, fx, fy);
     if (C.zsp) {
-      const double iso[6] = {g.a1, g.a2, g.a3, g.b1, g.b2, g.b3};
-      force_sp(__ldg(C.pmeritreg + ireg), rho, cs2h, xh, yh, iso, F.spmass[iel], fx, fy);
+#if BL_FAST_ALGEBRA
+      force_sp_iso(__ldg(C.pmeritreg + ireg), rho, cs2h, g.cross, g.ts, g.td, g.a1, g.a2, g.a3,
+                   g.b1, g.b2, g.b3, F.spmass[iel], fx, fy);
+#else
+      force_sp(__ldg(C.pmeritreg + ireg), rho, cs2h, xh, yh, F.spmass[iel], fx, fy);
+#endif
     }
     if (C.zhg) force_hg(__ldg(C.kappareg + ireg), rho, g.vol, S->rdt, u, v, fx, fy);
   }
