@@ -528,6 +528,11 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
       // written as s -+ a1 +- a2 -+ a3, exact in real arithmetic), from the
       // element's iso-parametric coefficients at these vertices
       const double ga1 = F.a1[iel], ga3 = F.a3[iel], gb1 = F.b1[iel], gb3 = F.b3[iel];
+      // |c|^2 of faces 1,3 and of faces 0,2 (only the cut test uses it)
+      const double c1sq = ga1 * ga1 + gb1 * gb1, c3sq = ga3 * ga3 + gb3 * gb3;
+      // max over faces of edv * |du|; the reference's max of
+      // edv * 2|du| / max(rho, zerocut) is that times 2 / max(rho, zerocut)
+      double vmax = 0.0;
 #else
       const double xc = quarter(x[0] + x[1] + x[2] + x[3]);
       const double yc = quarter(y[0] + y[1] + y[2] + y[3]);
@@ -554,6 +559,18 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
           double w1 = u[jn] - u[is], w2 = v[jn] - v[is];
           double w3 = x[jn] - x[is], w4 = y[jn] - y[is];
           const double du = w1, dv = w2;
+#if BL_FAST_ALGEBRA
+          // the face vectors' projections on their own unit vectors are
+          // |d|^2 / max(|d|, zerocut) (exact in real arithmetic, and never
+          // negative, so the reference's sign guards drop out)
+          const double squ = w1 * w1 + w2 * w2, sqx = w3 * w3 + w4 * w4;
+          const double lu = SQRT(squ), lx = SQRT(sqx);
+          const double ru = DIV(1.0, maxF_nn(lu, zc)), rx = DIV(1.0, maxF_nn(lx, zc));
+          const double uhat = w1 * ru, vhat = w2 * ru;
+          const double xh = w3 * rx, yh = w4 * rx;
+          w1 = DIV(squ * ru, maxF_nn(sqx * rx, zc));
+          w1 = DIV(1.0, maxF_nn(w1, zc));
+#else
           double den = SQRT(w1 * w1 + w2 * w2);
           const double lu = den;
           den = DIV(1.0, maxF_nn(den, zc));
@@ -565,6 +582,7 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
           den = w3 * xh + w4 * yh;
           w1 = DIV(w1 * uhat + w2 * vhat, signF(maxF_nn(absF(den), zc), den));
           w1 = DIV(1.0, signF(maxF_nn(absF(w1), zc), w1));
+#endif
           // neighbour faces: edge 1 uses MOD(ielfc,4)+1 / MOD(ielfc+2,4)+1,
           // edge 2 the other pair (hydro_kn_edgeviscosity.f90:117-151)
           const int ins1 = e2 == 0 ? ((f1 + 1) & 3) : ((f1 + 3) & 3);
@@ -600,8 +618,12 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
           w4 = lu;
           w3 = half(1.0 - w2) * (rho0 + F.rho[ins]) * (w1 + C.cvisc2 * w4);
           const double edv = w3;
+#if BL_FAST_ALGEBRA
+          vmax = maxF_nn(vmax, w3 * w4);  // never negative
+#else
           w4 = DIV(twice(w4), maxF(rho0, zc));
           visc = maxF_nn(visc, w3 * w4);  // visc stays +0 or positive
+#endif
           // edge force (hydro_kn_edgeviscosity.f90:219-282)
 #if BL_FAST_ALGEBRA
           {
@@ -615,13 +637,13 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
             const long long sb = bits64(w33) & (long long)0x8000000000000000ull;
             const double exh = from_bits64(bits64(cy) ^ (long long)0x8000000000000000ull ^ sb);
             const double eyh = from_bits64(bits64(cx) ^ sb);
-            const double w7sq = cx * cx + cy * cy;
+            const double w7sq = (is & 1) ? c1sq : c3sq;
             const double w8 = lx;
             const double w5 = lu;
             const double w6b = du * exh + dv * eyh;
-            const double d = DIV(w6b, maxF_nn(w5, zc));
-            edx[is] = edv * du * d;
-            edy[is] = edv * dv * d;
+            const double d = edv * DIV(w6b, maxF_nn(w5, zc));
+            edx[is] = du * d;
+            edy[is] = dv * d;
             if (le_nn(w5, zc) || geF(zc, w6b) || le_nn(w7sq, zc * zc) || le_nn(w8, zc)) {
               edx[is] = 0.0;
               edy[is] = 0.0;
@@ -654,6 +676,9 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
 #endif
         }
       }
+#if BL_FAST_ALGEBRA
+      visc = vmax * DIV(2.0, maxF(rho0, zc));
+#endif
       qx[0] = edx[0] - edx[3];
       qx[1] = edx[1] - edx[0];
       qx[2] = edx[2] - edx[1];
