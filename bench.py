@@ -17,9 +17,9 @@ e2e        the same metric through the reference-facing C-ABI with host
            each of bl_getdt/bl_lagstep(/bl_alestep) and bl_sync_to_host of
            the whole state, all inside the timed region.
 roofline   the dominant kernel (edge viscosity + dt, k_getdt) against the
-           measured HBM copy bandwidth, with algorithmic bytes per zone from
-           the phase table in DESIGN.md; "fp64" reports the binding FP64
-           issue roof.
+           measured HBM copy bandwidth, with algorithmic bytes per zone
+           (each field read once plus each field written once); "fp64"
+           reports the binding FP64 issue roof.
 cpu_baseline  the CPU restatement on this host's cores, a bounded sample
            of the same workload.
 
@@ -40,17 +40,19 @@ import time
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
-# algorithmic bytes per zone-cycle (phase table)
+# algorithmic bytes per zone-cycle: each field a phase reads counted once
+# plus each field it writes counted once (FP64 8 B, INT32 4 B, node fields
+# per node)
 B_LAG = 724
 B_EUL = 1628
 B_GETDT = 164
 # From the ncu capture of k_getdt at the end-of-run state (t = 1) of the
-# default workload (profiles/k_getdt_sedov512.md): the FP64-pipe instructions
-# (DFMA+DMUL+DADD+DSETP) it executes per zone, which with the FMA rate
-# measured live below place k_getdt against the FP64 issue roof that binds
-# it, and its DRAM traffic per launch (dram__bytes_read + _write).
-FP64_PER_ZONE_GETDT = 290
-TRAFFIC_GETDT_BYTES = 35.3e6
+# default workload: the FP64-pipe instructions (DFMA+DMUL+DADD+DSETP) it
+# executes per zone, which with the FMA rate measured live below place
+# k_getdt against the FP64 issue roof that binds it, and its DRAM traffic
+# per launch (dram__bytes_read + _write).
+FP64_PER_ZONE_GETDT = 269.5
+TRAFFIC_GETDT_BYTES = 45.7e6
 
 
 def workload_deck(name, size):
@@ -263,29 +265,18 @@ def main():
     value, t_max, _ = job_rate(ms, nel * nsteps, device="cuda")
     p.timestep = ts
 
-    # ---------------- dominant kernel: k_getdt timed alone -----------------
-    # (one getdt launch per call; the state is the one the run left).  The
-    # profiler range brackets these launches only, so that an ncu capture
-    # with --profile-from-start off sees k_getdt at the end-of-run state.
-    k_ms = []
+    # ---------------- per-kernel durations at the end-of-run state --------
+    # 16 more steps at the state the run left, the four kernels of each
+    # queued back to back on the library's stream with CUDA events between
+    # them (no host copies): the mean duration of each kernel.  The profiler
+    # range brackets these launches only, so that an ncu capture with
+    # --profile-from-start off sees the same launches.
     torch.cuda.profiler.start()
-    for _ in range(3):
-        q0 = torch.cuda.Event(enable_timing=True)
-        q1 = torch.cuda.Event(enable_timing=True)
-        ts = p.timestep.copy()
-        q0.record(stream)
-        s.inf_solver_getdt(ts)
-        q1.record(stream)
-        q1.synchronize()
-        k_ms.append(q0.elapsed_time(q1))
-    # one lagstep (force, accel, state) at the same state, also timed alone
-    q0.record(stream)
-    s.inf_solver_lagstep(ts)
-    q1.record(stream)
-    q1.synchronize()
-    lag_ms = q0.elapsed_time(q1)
+    ierr_k, kms = s.time_step_kernels(16, p.timestep.copy())
     torch.cuda.profiler.stop()
-    k_ms = sorted(k_ms)[1]
+    assert ierr_k == 0, s.error.message
+    k_ms = kms[0]
+    lag_ms = kms[1] + kms[2] + kms[3]
     hbm_peak, peak_kind = load_peaks()
     achieved = B_GETDT * nel / (k_ms * 1e-3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
@@ -294,7 +285,11 @@ def main():
             "kernel": "k_getdt",
             "peak_kind": peak_kind, "kernel_ms": k_ms,
             "note": "the FP64 issue rate, not HBM, bounds this path; see fp64",
-            "lagstep_ms_alone": lag_ms}
+            "lagstep_ms": lag_ms,
+            "kernels_ms": {"k_getdt": kms[0], "k_lag_force": kms[1], "k_lag_accel": kms[2],
+                           "k_lag_state": kms[3],
+                           "how": "mean of 16 steps after the timed run, CUDA events between "
+                                  "the kernels on the library's stream"}}
     step_bytes = bytes_zc * nel
     from bookleaf_f90_gb300 import _lib
     rates = _lib.fp64_rates()

@@ -741,6 +741,74 @@ int bl_run(bl_ctx* x, bl_timestep* ts, int max_steps, bl_step_record* history, i
   return BL_SUCCESS;
 }
 
+// Per-kernel durations of the Lagrangian step: the four kernels of nstep
+// steps are queued back to back with an event between each (the per-call
+// path's header, so the end time does not stop them), then timed from the
+// events once the last one has completed.
+int bl_time_step_kernels(bl_ctx* x, bl_timestep* ts, int nstep, double* ms, int n, bl_error* e) {
+  set_err(e, BL_SUCCESS, BL_HALT_SINGLE, "");
+  constexpr int kMaxSteps = 64;
+  if (!x || !ts || !ms || n < 4 || nstep < 1 || nstep > kMaxSteps) {
+    set_err(e, BL_FAILURE, BL_HALT_ALL,
+            "ERROR: bl_time_step_kernels: bad argument (nstep 1..64, n >= 4)");
+    return BL_FAILURE;
+  }
+  std::vector<cudaEvent_t> ev(4 * nstep + 1, nullptr);
+  cudaError_t r = cudaSuccess;
+  for (auto& v : ev)
+    if (r == cudaSuccess) r = cudaEventCreate(&v);
+  auto release = [&]() {
+    for (auto& v : ev)
+      if (v) cudaEventDestroy(v);
+  };
+  if (r != cudaSuccess) {
+    release();
+    return cuda_fail(e, r, "bl_time_step_kernels");
+  }
+  header_from_ts(x, ts, 0);
+  cudaEventRecord(ev[0], x->stream);
+  for (int k = 0; k < nstep; k++) {
+    x->L.getdt(x->F, x->C, x->stream);
+    cudaEventRecord(ev[4 * k + 1], x->stream);
+    x->L.lag_force(x->F, x->C, x->stream);
+    cudaEventRecord(ev[4 * k + 2], x->stream);
+    x->L.lag_accel(x->F, x->C, x->stream);
+    cudaEventRecord(ev[4 * k + 3], x->stream);
+    x->L.lag_state(x->F, x->C, x->stream);
+    cudaEventRecord(ev[4 * k + 4], x->stream);
+  }
+  x->launches += (long long)nstep * (bl::kLaunchesGetdt + bl::kLaunchesLagstep);
+  r = cudaEventSynchronize(ev[4 * nstep]);
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int k = 0; k < nstep && r == cudaSuccess; k++)
+    for (int j = 0; j < 4 && r == cudaSuccess; j++) {
+      float t = 0.0f;
+      r = cudaEventElapsedTime(&t, ev[4 * k + j], ev[4 * k + j + 1]);
+      acc[j] += t;
+    }
+  release();
+  if (r != cudaSuccess) return cuda_fail(e, r, "bl_time_step_kernels");
+  for (int j = 0; j < 4; j++) ms[j] = acc[j] / nstep;
+  int rc = fetch_header(x, e, "bl_time_step_kernels");
+  if (rc != BL_SUCCESS) return rc;
+  const DevStep S = *x->hstep;
+  x->cs2_is_v = false;
+  fill_ts_from_step(x, S, ts);
+  ts->zcorrector = 1;
+  ts->dts = ts->dt;
+  if (S.err_code == 1) {
+    set_err(e, BL_FAILURE, BL_HALT_SINGLE, "ERROR: negative CFL condition in hydro_dr_getdt");
+    return BL_FAILURE;
+  }
+  if (S.err_code == 2) {
+    set_err(e, BL_FAILURE, BL_HALT_ALL, "ERROR: dt < dt_min");
+    return BL_FAILURE;
+  }
+  if (S.negvol_pred) return negvol_error(S.negvol_pred, e);
+  if (S.negvol_corr) return negvol_error(S.negvol_corr, e);
+  return BL_SUCCESS;
+}
+
 static size_t field_count(const bl_ctx* x, int id, int& kind) {
   // kind: 0 double element, 1 double corner, 2 double node, 3 double comp,
   //       4 derived (cnx/cny/cpa*), -1 not a device state field

@@ -59,12 +59,14 @@ static __device__ __noinline__ double dsqrt_call(double x) { return dsqrt_rn(x);
 
 // Resident blocks of 128 threads per SM the two heaviest kernels are
 // compiled for (register budget 65536 / (128 * n) per thread).  Chosen by
-// timing the whole Sedov 512x512 run on the GB300 over n = 3..6: k_getdt
-// gains from more warps to hide its integer-pipe divide chains (5 blocks,
-// 102 registers), k_lag_force from fewer spills (3 blocks): 414.5M
-// zone-cycles/s against 393.3M with 4 and 4.
+// timing the whole Sedov 512x512 run on the GB300 over k_getdt n = 5..8
+// and k_lag_force n = 2..6: 832.0M zone-cycles/s at 7 and 4 against 814.9M
+// at 5 and 3, 822.0M at 7 and 3, 823.4M at 5 and 4.  k_getdt gains from
+// the warps that hide its integer-pipe divide chains and from the 8,192
+// warps of a 512x512 mesh filling 1.92 waves of 28 warps per SM instead of
+// 2.69 waves of 20 (the last, part-filled wave drains at low occupancy).
 #ifndef BL_GETDT_MINB
-#define BL_GETDT_MINB 5
+#define BL_GETDT_MINB 7
 #endif
 // The fast build may also use exact algebraic identities that can change
 // only the sign of a zero (negation symmetry of opposite corners); the
@@ -73,7 +75,7 @@ static __device__ __noinline__ double dsqrt_call(double x) { return dsqrt_rn(x);
 #define BL_FAST_ALGEBRA 0
 #endif
 #ifndef BL_FORCE_MINB
-#define BL_FORCE_MINB 3
+#define BL_FORCE_MINB 4
 #endif
 
 namespace bl {
@@ -773,9 +775,33 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
   cfli = 0x7fffffff;
   divv = DBL_MIN;
   divi = -1;
-  for (int b = threadIdx.x; b < (int)gridDim.x; b += BS) {
-    cfl_min(cflv, cfli, ((volatile double*)F.red_v)[2 * b], ((volatile int*)F.red_i)[2 * b]);
-    div_max(divv, divi, ((volatile double*)F.red_v)[2 * b + 1], ((volatile int*)F.red_i)[2 * b + 1]);
+  // Each thread takes the partials b = tid, tid + BS, ... in that order as
+  // before, eight at a time: their loads (L2, past the L1 that may not see
+  // other blocks' writes) are all in flight before the first comparison.
+  {
+    constexpr int U = 8;
+    const double2* rv = reinterpret_cast<const double2*>(F.red_v);
+    const int2* ri = reinterpret_cast<const int2*>(F.red_i);
+    const int nb = (int)gridDim.x;
+    for (int b0 = threadIdx.x; b0 < nb; b0 += BS * U) {
+      double2 v[U];
+      int2 ix[U];
+#pragma unroll
+      for (int t = 0; t < U; t++) {
+        const int b = b0 + t * BS;
+        if (b < nb) {
+          v[t] = __ldcg(rv + b);
+          ix[t] = __ldcg(ri + b);
+        }
+      }
+#pragma unroll
+      for (int t = 0; t < U; t++) {
+        if (b0 + t * BS < nb) {
+          cfl_min(cflv, cfli, v[t].x, ix[t].x);
+          div_max(divv, divi, v[t].y, ix[t].y);
+        }
+      }
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {

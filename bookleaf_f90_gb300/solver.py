@@ -116,6 +116,16 @@ class Solver:
     def stream(self):
         return self.L.bl_stream(self.ctx)
 
+    def time_step_kernels(self, nstep=16, ts=None):
+        """Advances nstep Lagrangian steps with the four kernels queued back
+        to back and CUDA events between them; returns (ierr, [ms of getdt,
+        lag_force, lag_accel, lag_state], each the mean over the steps)."""
+        ts = ts or self.timestep
+        ms = (ct.c_double * 4)()
+        ierr = self.L.bl_time_step_kernels(self.ctx, ct.byref(ts), int(nstep), ms, 4,
+                                           ct.byref(self.error))
+        return ierr, list(ms)
+
     @property
     def kernel_launches(self):
         return self.L.bl_kernel_launches(self.ctx)

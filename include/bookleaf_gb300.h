@@ -208,6 +208,20 @@ void *bl_stream(bl_ctx *ctx);
 /* Number of kernels this context has launched so far. */
 long long bl_kernel_launches(bl_ctx *ctx);
 
+/* Durations of the kernels of a Lagrangian step at the context's current
+ * state (no counterpart in the reference; a measurement aid).  Advances
+ * the state by nstep steps (1..64) from *ts: the kernels of the getdt and
+ * lagstep entry points are queued back to back on the context's stream
+ * with a CUDA event between each and no host copy between steps, without
+ * the end-time stop of bl_run (so it also runs past time_end).  ms[0..3]
+ * (n >= 4) receive the mean durations in milliseconds of the getdt
+ * kernel and of the three lagstep kernels (force, acceleration, state);
+ * *ts receives the state after the last step.  The ALE step is not run.
+ * Returns BL_SUCCESS, or BL_FAILURE with *err set as the solver entry
+ * points set it. */
+int bl_time_step_kernels(bl_ctx *ctx, bl_timestep *ts, int nstep, double *ms, int n,
+                         bl_error *err);
+
 /* Library version string. */
 const char *bl_version(void);
 

@@ -222,3 +222,25 @@ def test_dt_min_halt():
     assert s.error.iout == abi.HALT_ALL
     assert s.error.message == "ERROR: dt < dt_min"
     assert p.timestep.nstep == 1   # time_dr_end updates before the check
+
+
+def test_time_step_kernels_advances_like_the_device_loop():
+    """bl_time_step_kernels (the per-kernel timing aid) runs the same
+    kernels in the same order as bl_run: after 8 steps the state equals the
+    device loop's bit for bit, and every kernel reports a positive time."""
+    base = Problem.from_deck(configs.sedov(24, kappa=0.01, pmerit=0.1))
+    pa, pb = base.copy(), base.copy()
+    sa = Solver(pa, fp_mode=abi.FP_EXACT)
+    ierr, ms = sa.time_step_kernels(8)
+    assert ierr == 0, sa.error.message
+    assert len(ms) == 4 and all(m > 0.0 for m in ms)
+    sb = Solver(pb, fp_mode=abi.FP_EXACT)
+    ierr, _ = sb.run(max_steps=8, history=False)
+    assert ierr == 0
+    assert (pa.timestep.nstep, pa.timestep.time, pa.timestep.dt) == (
+        pb.timestep.nstep, pb.timestep.time, pb.timestep.dt)
+    sa.sync_to_host(0)
+    sb.sync_to_host(0)
+    assert not compare(pa, pb, exact=True)
+    ierr, _ = sa.time_step_kernels(65)
+    assert ierr != 0 and "bad argument" in sa.error.message
