@@ -51,8 +51,8 @@ B_GETDT = 164
 # executes per zone, which with the FMA rate measured live below place
 # k_getdt against the FP64 issue roof that binds it, and its DRAM traffic
 # per launch (dram__bytes_read + _write).
-FP64_PER_ZONE_GETDT = 269.5
-TRAFFIC_GETDT_BYTES = 45.7e6
+FP64_PER_ZONE_GETDT = 226.9
+TRAFFIC_GETDT_BYTES = 50.9e6
 
 
 def workload_deck(name, size):

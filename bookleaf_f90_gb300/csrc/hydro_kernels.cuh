@@ -483,256 +483,55 @@ __device__ __forceinline__ void div_max(double& v, int& i, double ov, int oi) {
   if (io > iv || (io == iv && oi >= 0 && (i < 0 || oi < i))) { v = ov; i = oi; }
 }
 
+// hydro_dr_getcs2 (elcs2 += elvisc; mixed cells: sum frmass*(cpcs2+cpvisc)),
+// then the element's hydro_kn_getdtcfl and getdtdiv candidates
+__device__ __forceinline__ void getdt_tail(const DevFields& F, const DevCfg& C, int iel,
+                                           const double* x, const double* y, const double* u,
+                                           const double* v, double visc, double& cflv, int& cfli,
+                                           double& divv, int& divi) {
+  double cs2v = F.cs2[iel] + visc;
+  const int imx = F.elmx ? F.elmx[iel] : -1;
+  if (imx >= 0) {
+    double w1 = 0.0;
+    const int c0 = F.imxfcp[imx], nc = F.imxncp[imx];
+    for (int k = 0; k < nc; k++) w1 = w1 + F.frm[c0 + k] * (F.cpcs2[c0 + k] + F.cpvisc[c0 + k]);
+    cs2v = w1;
+  }
+  F.cs2v[iel] = cs2v;
+  // hydro_kn_getdtcfl
+  const int ireg = __ldg(F.ielreg + iel);
+  double r11;
+  if (__ldg(C.zdtnotreg + ireg)) {
+    r11 = DBL_MAX;
+  } else {
+#if BL_FAST_ALGEBRA
+    double w1 = __ldg(C.zmidlength + ireg)
+                    ? min_dlm(x, y)
+                    : min_dln_iso(x, y, C.zcut, F.a1[iel], F.a2[iel], F.a3[iel], F.b1[iel],
+                                  F.b2[iel], F.b3[iel]);
+#else
+    double w1 = __ldg(C.zmidlength + ireg) ? min_dlm(x, y) : min_dln(x, y, C.zcut);
+#endif
+    r11 = DIV(w1, cs2v);
+  }
+  cflv = r11;
+  cfli = iel;
+  // hydro_kn_getdtdiv
+  const double A1 = F.a1[iel], A3 = F.a3[iel], B1 = F.b1[iel], B3 = F.b3[iel];
+  double w1 = u[0] * (-B3 + B1) + v[0] * (A3 - A1) + u[1] * (B3 + B1) + v[1] * (-A3 - A1) +
+              u[2] * (B3 - B1) + v[2] * (-A3 + A1) + u[3] * (-B3 - B1) + v[3] * (A3 + A1);
+  w1 = DIV(absF(w1), F.vol[iel]);
+  if (gt_nn(w1, divv)) {  // divv is TINY or a larger positive value
+    divv = w1;
+    divi = iel;
+  }
+}
+
+// The block reduction of the candidates, the last block's reduction of the
+// block partials and time_dr_end (time_dr_advance.f90:74-132)
 template <int BS>
-__global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg C) {
-  DevStep* S = F.step;
-  if (halted(S)) return;
-  if (S->stop_next) {            // bl_run: the previous step reached time_end
-    if (blockIdx.x == 0 && threadIdx.x == 0) S->halted = 1;
-    return;
-  }
-  const int iel = blockIdx.x * BS + threadIdx.x;
-  double cflv = HUGE_VAL;        // sentinel above HUGE(1.0)
-  int cfli = 0x7fffffff;
-  double divv = DBL_MIN;         // TINY(1.0)
-  int divi = -1;
-  if (iel < F.nel) {
-    const int4 nd = __ldg(F.ielnd + iel);
-    const int n[4] = {nd.x, nd.y, nd.z, nd.w};
-    double x[4], y[4], u[4], v[4];
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-      x[j] = F.ndx[n[j]];
-      y[j] = F.ndy[n[j]];
-      u[j] = F.ndu[n[j]];
-      v[j] = F.ndv[n[j]];
-    }
-    const double zc = C.zerocut;
-    const double rho0 = F.rho[iel];
-    double visc = 0.0;
-    double qx[4] = {0.0, 0.0, 0.0, 0.0}, qy[4] = {0.0, 0.0, 0.0, 0.0};
-    if (!C.ztq) {
-      // hydro_kn_initeviscosity / limiteviscosity / geteviscosity
-      // (hydro_kn_edgeviscosity.f90:30-282), evaluated face by face: every
-      // quantity of a face -- its differences (face j runs corner j ->
-      // j+1), lengths, normalised vectors, limiter ratios, edge coefficient
-      // and edge force -- is formed and consumed before the next face, which
-      // keeps the live state to the element's corners and the four edge
-      // forces.  The faces of side s (neighbours across faces s and s+2)
-      // are (s+3)&3 and s+1, in the reference's order 3, 1, 0, 2.
-      const int4 ee = __ldg(F.ielel + iel);
-      const int nb[4] = {ee.x, ee.y, ee.z, ee.w};
-      const int fcp = __ldg(F.ielfc + iel);
-      const double cs2i = F.cs2[iel];
-#if BL_FAST_ALGEBRA
-      // fast build: the vector from an edge's midpoint to the centroid is
-      // (a3,b3), (-a1,-b1), (-a3,-b3), (a1,b1) for faces 0..3 (corners
-      // written as s -+ a1 +- a2 -+ a3, exact in real arithmetic), from the
-      // element's iso-parametric coefficients at these vertices
-      const double ga1 = F.a1[iel], ga3 = F.a3[iel], gb1 = F.b1[iel], gb3 = F.b3[iel];
-      // |c|^2 of faces 1,3 and of faces 0,2 (only the cut test uses it)
-      const double c1sq = ga1 * ga1 + gb1 * gb1, c3sq = ga3 * ga3 + gb3 * gb3;
-      // max over faces of edv * |du|; the reference's max of
-      // edv * 2|du| / max(rho, zerocut) is that times 2 / max(rho, zerocut)
-      double vmax = 0.0;
-#else
-      const double xc = quarter(x[0] + x[1] + x[2] + x[3]);
-      const double yc = quarter(y[0] + y[1] + y[2] + y[3]);
-#endif
-      double edx[4], edy[4];
-#pragma unroll
-      for (int s = 0; s < 2; s++) {
-        const int in1 = nb[s], in2 = nb[s + 2];
-        const int f1 = fc_of(fcp, s), f2 = fc_of(fcp, s + 2);
-        // boundary rule (hydro_kn_edgeviscosity.f90:154-183): a ratio across
-        // a boundary face is 1 between two boundary nodes facing an
-        // interior neighbour, 0 otherwise
-        double val1 = 0.0, val2 = 0.0;
-        if (in1 == iel)
-          val1 = (__ldg(F.indtype + n[s]) < 0 && __ldg(F.indtype + n[(s + 1) & 3]) < 0 && in2 != iel)
-                     ? 1.0 : 0.0;
-        if (in2 == iel)
-          val2 = (__ldg(F.indtype + n[s + 2]) < 0 && __ldg(F.indtype + n[(s + 3) & 3]) < 0 &&
-                  in1 != iel) ? 1.0 : 0.0;
-#pragma unroll
-        for (int e2 = 0; e2 < 2; e2++) {
-          const int is = e2 == 0 ? ((s + 3) & 3) : (s + 1);
-          const int jn = (is + 1) & 3;
-          double w1 = u[jn] - u[is], w2 = v[jn] - v[is];
-          double w3 = x[jn] - x[is], w4 = y[jn] - y[is];
-          const double du = w1, dv = w2;
-#if BL_FAST_ALGEBRA
-          // the face vectors' projections on their own unit vectors are
-          // |d|^2 / max(|d|, zerocut) (exact in real arithmetic, and never
-          // negative, so the reference's sign guards drop out)
-          const double squ = w1 * w1 + w2 * w2, sqx = w3 * w3 + w4 * w4;
-          const double lu = SQRT(squ), lx = SQRT(sqx);
-          const double ru = DIV(1.0, maxF_nn(lu, zc)), rx = DIV(1.0, maxF_nn(lx, zc));
-          const double uhat = w1 * ru, vhat = w2 * ru;
-          const double xh = w3 * rx, yh = w4 * rx;
-          w1 = DIV(squ * ru, maxF_nn(sqx * rx, zc));
-          w1 = DIV(1.0, maxF_nn(w1, zc));
-#else
-          double den = SQRT(w1 * w1 + w2 * w2);
-          const double lu = den;
-          den = DIV(1.0, maxF_nn(den, zc));
-          const double uhat = w1 * den, vhat = w2 * den;
-          den = SQRT(w3 * w3 + w4 * w4);
-          const double lx = den;
-          den = DIV(1.0, maxF_nn(den, zc));
-          const double xh = w3 * den, yh = w4 * den;
-          den = w3 * xh + w4 * yh;
-          w1 = DIV(w1 * uhat + w2 * vhat, signF(maxF_nn(absF(den), zc), den));
-          w1 = DIV(1.0, signF(maxF_nn(absF(w1), zc), w1));
-#endif
-          // neighbour faces: edge 1 uses MOD(ielfc,4)+1 / MOD(ielfc+2,4)+1,
-          // edge 2 the other pair (hydro_kn_edgeviscosity.f90:117-151)
-          const int ins1 = e2 == 0 ? ((f1 + 1) & 3) : ((f1 + 3) & 3);
-          const int ins2 = e2 == 0 ? ((f2 + 3) & 3) : ((f2 + 1) & 3);
-          double r1 = val1, r2 = val2;
-          if (in1 != iel) {
-            const int4 m = __ldg(F.ielnd + in1);
-            const int mm[4] = {m.x, m.y, m.z, m.w};
-            const int a = mm[ins1], b = mm[(ins1 + 1) & 3];
-            double ddx = F.ndx[b] - F.ndx[a], ddy = F.ndy[b] - F.ndy[a];
-            double ddu = F.ndu[b] - F.ndu[a], ddv = F.ndv[b] - F.ndv[a];
-            double dn = ddx * xh + ddy * yh;
-            double q = DIV(ddu * uhat + ddv * vhat, signF(maxF_nn(absF(dn), zc), dn));
-            r1 = q * w1;
-          }
-          if (in2 != iel) {
-            const int4 m = __ldg(F.ielnd + in2);
-            const int mm[4] = {m.x, m.y, m.z, m.w};
-            const int a = mm[ins2], b = mm[(ins2 + 1) & 3];
-            double ddx = F.ndx[b] - F.ndx[a], ddy = F.ndy[b] - F.ndy[a];
-            double ddu = F.ndu[b] - F.ndu[a], ddv = F.ndv[b] - F.ndv[a];
-            double dn = ddx * xh + ddy * yh;
-            double q = DIV(ddu * uhat + ddv * vhat, signF(maxF_nn(absF(dn), zc), dn));
-            r2 = q * w1;
-          }
-          // limiter and edge coefficient (hydro_kn_edgeviscosity.f90:185-214)
-          const int ins = nb[is];
-          w1 = C.cvisc1 * SQRT(half(cs2i + F.cs2[ins]));
-          w2 = r1;
-          w3 = r2;
-          w2 = minF(minF(minF(half(w2 + w3), twice(w2)), twice(w3)), 1.0);
-          w2 = maxF(0.0, w2);
-          w4 = lu;
-          w3 = half(1.0 - w2) * (rho0 + F.rho[ins]) * (w1 + C.cvisc2 * w4);
-          const double edv = w3;
-#if BL_FAST_ALGEBRA
-          vmax = maxF_nn(vmax, w3 * w4);  // never negative
-#else
-          w4 = DIV(twice(w4), maxF(rho0, zc));
-          visc = maxF_nn(visc, w3 * w4);  // visc stays +0 or positive
-#endif
-          // edge force (hydro_kn_edgeviscosity.f90:219-282)
-#if BL_FAST_ALGEBRA
-          {
-            // the reference normalises the midpoint-to-centroid vector c,
-            // orients it by the sign of its product with the face vector and
-            // scales it back by |c|: (exh, eyh) = -+(cy, -cx), the sign bit
-            // of w33 = cy*xh - cx*yh choosing; |c| only enters the cut test
-            const double cx = is == 0 ? ga3 : (is == 1 ? negF(ga1) : (is == 2 ? negF(ga3) : ga1));
-            const double cy = is == 0 ? gb3 : (is == 1 ? negF(gb1) : (is == 2 ? negF(gb3) : gb1));
-            const double w33 = cy * xh - cx * yh;
-            const long long sb = bits64(w33) & (long long)0x8000000000000000ull;
-            const double exh = from_bits64(bits64(cy) ^ (long long)0x8000000000000000ull ^ sb);
-            const double eyh = from_bits64(bits64(cx) ^ sb);
-            const double w7sq = (is & 1) ? c1sq : c3sq;
-            const double w8 = lx;
-            const double w5 = lu;
-            const double w6b = du * exh + dv * eyh;
-            const double d = edv * DIV(w6b, maxF_nn(w5, zc));
-            edx[is] = du * d;
-            edy[is] = dv * d;
-            if (le_nn(w5, zc) || geF(zc, w6b) || le_nn(w7sq, zc * zc) || le_nn(w8, zc)) {
-              edx[is] = 0.0;
-              edy[is] = 0.0;
-            }
-          }
-#else
-          {
-            const double m3 = half(x[is] + x[jn]);
-            const double m6 = half(y[is] + y[jn]);
-            const double w7 = SQRT((xc - m3) * (xc - m3) + (yc - m6) * (yc - m6));
-            const double w8 = lx;  // SQRT(w1*w1+w4*w4) of the same face difference
-            double d = DIV(1.0, w7);
-            double exh = (yc - m6) * d, eyh = (m3 - xc) * d;
-            // w1*(1/w8), w4*(1/w8): the limiter's normalised face vector
-            // whenever w8 > zerocut; otherwise the edge is cut below
-            const double w33 = exh * xh + eyh * yh;
-            d = -(signF(1.0, w33) * w7);
-            exh = exh * d;
-            eyh = eyh * d;
-            const double w5 = lu;
-            const double w6b = du * exh + dv * eyh;
-            d = DIV(w6b, maxF_nn(w5, zc));
-            edx[is] = edv * du * d;
-            edy[is] = edv * dv * d;
-            if (le_nn(w5, zc) || geF(zc, w6b) || le_nn(w7, zc) || le_nn(w8, zc)) {
-              edx[is] = 0.0;
-              edy[is] = 0.0;
-            }
-          }
-#endif
-        }
-      }
-#if BL_FAST_ALGEBRA
-      visc = vmax * DIV(2.0, maxF(rho0, zc));
-#endif
-      qx[0] = edx[0] - edx[3];
-      qx[1] = edx[1] - edx[0];
-      qx[2] = edx[2] - edx[1];
-      qx[3] = edx[3] - edx[2];
-      qy[0] = edy[0] - edy[3];
-      qy[1] = edy[1] - edy[0];
-      qy[2] = edy[2] - edy[1];
-      qy[3] = edy[3] - edy[2];
-      F.cnviscx[iel] = make_d4(qx[0], qx[1], qx[2], qx[3]);
-      F.cnviscy[iel] = make_d4(qy[0], qy[1], qy[2], qy[3]);
-      F.visc[iel] = visc;
-    } else {
-      visc = F.visc[iel];
-    }
-    // hydro_dr_getcs2: elcs2 += elvisc; mixed cells: sum frmass*(cpcs2+cpvisc)
-    double cs2v = F.cs2[iel] + visc;
-    const int imx = F.elmx ? F.elmx[iel] : -1;
-    if (imx >= 0) {
-      double w1 = 0.0;
-      const int c0 = F.imxfcp[imx], nc = F.imxncp[imx];
-      for (int k = 0; k < nc; k++) w1 = w1 + F.frm[c0 + k] * (F.cpcs2[c0 + k] + F.cpvisc[c0 + k]);
-      cs2v = w1;
-    }
-    F.cs2v[iel] = cs2v;
-    // hydro_kn_getdtcfl
-    const int ireg = __ldg(F.ielreg + iel);
-    double r11;
-    if (__ldg(C.zdtnotreg + ireg)) {
-      r11 = DBL_MAX;
-    } else {
-#if BL_FAST_ALGEBRA
-      double w1 = __ldg(C.zmidlength + ireg)
-                      ? min_dlm(x, y)
-                      : min_dln_iso(x, y, C.zcut, F.a1[iel], F.a2[iel], F.a3[iel], F.b1[iel],
-                                    F.b2[iel], F.b3[iel]);
-#else
-      double w1 = __ldg(C.zmidlength + ireg) ? min_dlm(x, y) : min_dln(x, y, C.zcut);
-#endif
-      r11 = DIV(w1, cs2v);
-    }
-    cflv = r11;
-    cfli = iel;
-    // hydro_kn_getdtdiv
-    const double A1 = F.a1[iel], A3 = F.a3[iel], B1 = F.b1[iel], B3 = F.b3[iel];
-    double w1 = u[0] * (-B3 + B1) + v[0] * (A3 - A1) + u[1] * (B3 + B1) + v[1] * (-A3 - A1) +
-                u[2] * (B3 - B1) + v[2] * (-A3 + A1) + u[3] * (-B3 - B1) + v[3] * (A3 + A1);
-    w1 = DIV(absF(w1), F.vol[iel]);
-    if (gt_nn(w1, divv)) {  // divv is TINY or a larger positive value
-      divv = w1;
-      divi = iel;
-    }
-  }
+__device__ __forceinline__ void getdt_finish(const DevFields& F, const DevCfg& C, DevStep* S,
+                                             double cflv, int cfli, double divv, int divi) {
   // ---- block reduction
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -873,6 +672,420 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
     S->nrecord = r + 1;
   }
 }
+
+#if BL_FAST_ALGEBRA
+// Fast build.  The quantities of a face that both elements sharing it
+// compute -- its lengths, unit vectors and the inverse ratio of its
+// projections -- from the face's velocity (du, dv) and position (dx, dy)
+// differences; the face vectors' projections on their own unit vectors
+// are |d|^2 / max(|d|, zerocut) (exact in real arithmetic, never negative,
+// so the reference's sign guards drop out).
+struct FaceQ {
+  double du, dv, lu, lx, uh, vh, xh, yh, w1;
+};
+__device__ __forceinline__ FaceQ face_q(double du, double dv, double dx, double dy, double zc) {
+  FaceQ f;
+  f.du = du;
+  f.dv = dv;
+  const double squ = du * du + dv * dv, sqx = dx * dx + dy * dy;
+  f.lu = SQRT(squ);
+  f.lx = SQRT(sqx);
+  const double ru = DIV(1.0, maxF_nn(f.lu, zc)), rx = DIV(1.0, maxF_nn(f.lx, zc));
+  f.uh = du * ru;
+  f.vh = dv * ru;
+  f.xh = dx * rx;
+  f.yh = dy * rx;
+  const double w1 = DIV(squ * ru, maxF_nn(sqx * rx, zc));
+  f.w1 = DIV(1.0, maxF_nn(w1, zc));
+  return f;
+}
+// limiter ratio of a neighbour face with differences (ddx, ddy, ddu, ddv)
+// against face f (hydro_kn_edgeviscosity.f90:117-151)
+__device__ __forceinline__ double nb_ratio(const FaceQ& f, double ddx, double ddy, double ddu,
+                                           double ddv, double zc) {
+  const double dn = ddx * f.xh + ddy * f.yh;
+  const double q = DIV(ddu * f.uh + ddv * f.vh, signF(maxF_nn(absF(dn), zc), dn));
+  return q * f.w1;
+}
+
+// k_getdt of the fast build shares face work between neighbouring threads.
+// A block of BS threads takes BS - 2 consecutive elements; thread t holds
+// element blockIdx*(BS-2) + t - 1, so threads 0 and BS-1 hold the
+// neighbours of the block's first and last elements (halos).  Every
+// thread first publishes in shared memory the quantities of its face 0 and
+// the differences of its faces 1 and 3; then each element takes
+// - face 2 from the thread across it when that element is the adjacent one
+//   and the face is its face 0 (the same edge run the other way: the
+//   differences and unit vectors change sign, lengths and ratio do not);
+// - the differences of a neighbour face of the limiter from the adjacent
+//   thread when the neighbour is that element and the face is its face 1
+//   or 3 (the same arithmetic on the same operands);
+// and computes everything else itself, as the exact build does.  On the
+// generated meshes elements are numbered along mesh lines, so the face
+// across face 2 and the two limiter neighbours of side 0 are the adjacent
+// elements and take the shared path.
+template <int BS>
+__global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg C) {
+  DevStep* S = F.step;
+  if (halted(S)) return;
+  if (S->stop_next) {            // bl_run: the previous step reached time_end
+    if (blockIdx.x == 0 && threadIdx.x == 0) S->halted = 1;
+    return;
+  }
+  const int t = threadIdx.x;
+  const int iel = blockIdx.x * (BS - 2) + t - 1;
+  const bool inmesh = iel >= 0 && iel < F.nel;
+  const bool own = inmesh && t > 0 && t < BS - 1;
+  double cflv = HUGE_VAL;        // sentinel above HUGE(1.0)
+  int cfli = 0x7fffffff;
+  double divv = DBL_MIN;         // TINY(1.0)
+  int divi = -1;
+  __shared__ double s_f0[9][BS];  // face 0: du dv lu lx uh vh xh yh w1
+  __shared__ double s_fd[8][BS];  // faces 1, 3: dx dy du dv each
+  const double zc = C.zerocut;
+  int n[4] = {0, 0, 0, 0};
+  double x[4], y[4], u[4], v[4];
+  if (inmesh) {
+    const int4 nd = __ldg(F.ielnd + iel);
+    n[0] = nd.x;
+    n[1] = nd.y;
+    n[2] = nd.z;
+    n[3] = nd.w;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      x[j] = F.ndx[n[j]];
+      y[j] = F.ndy[n[j]];
+      u[j] = F.ndu[n[j]];
+      v[j] = F.ndv[n[j]];
+    }
+  }
+  if (!C.ztq) {
+    if (inmesh) {
+      const FaceQ f0 = face_q(u[1] - u[0], v[1] - v[0], x[1] - x[0], y[1] - y[0], zc);
+      s_f0[0][t] = f0.du;
+      s_f0[1][t] = f0.dv;
+      s_f0[2][t] = f0.lu;
+      s_f0[3][t] = f0.lx;
+      s_f0[4][t] = f0.uh;
+      s_f0[5][t] = f0.vh;
+      s_f0[6][t] = f0.xh;
+      s_f0[7][t] = f0.yh;
+      s_f0[8][t] = f0.w1;
+      s_fd[0][t] = x[2] - x[1];
+      s_fd[1][t] = y[2] - y[1];
+      s_fd[2][t] = u[2] - u[1];
+      s_fd[3][t] = v[2] - v[1];
+      s_fd[4][t] = x[0] - x[3];
+      s_fd[5][t] = y[0] - y[3];
+      s_fd[6][t] = u[0] - u[3];
+      s_fd[7][t] = v[0] - v[3];
+    }
+    __syncthreads();
+  }
+  if (own) {
+    const double rho0 = F.rho[iel];
+    double visc = 0.0;
+    if (!C.ztq) {
+      // hydro_kn_initeviscosity / limiteviscosity / geteviscosity
+      // (hydro_kn_edgeviscosity.f90:30-282), face by face in the reference's
+      // order 3, 1, 0, 2 (the faces of side s are (s+3)&3 and s+1)
+      const int4 ee = __ldg(F.ielel + iel);
+      const int nb[4] = {ee.x, ee.y, ee.z, ee.w};
+      const int fcp = __ldg(F.ielfc + iel);
+      const double cs2i = F.cs2[iel];
+      // the vector from an edge's midpoint to the centroid is (a3,b3),
+      // (-a1,-b1), (-a3,-b3), (a1,b1) for faces 0..3 (corners written as
+      // s -+ a1 +- a2 -+ a3, exact in real arithmetic)
+      const double ga1 = F.a1[iel], ga3 = F.a3[iel], gb1 = F.b1[iel], gb3 = F.b3[iel];
+      // |c|^2 of faces 1,3 and of faces 0,2 (only the cut test uses it)
+      const double c1sq = ga1 * ga1 + gb1 * gb1, c3sq = ga3 * ga3 + gb3 * gb3;
+      // max over faces of edv * |du|; the reference's max of
+      // edv * 2|du| / max(rho, zerocut) is that times 2 / max(rho, zerocut)
+      double vmax = 0.0;
+      double edx[4], edy[4];
+#pragma unroll
+      for (int s = 0; s < 2; s++) {
+        const int in1 = nb[s], in2 = nb[s + 2];
+        const int f1 = fc_of(fcp, s), f2 = fc_of(fcp, s + 2);
+        // boundary rule (hydro_kn_edgeviscosity.f90:154-183)
+        double val1 = 0.0, val2 = 0.0;
+        if (in1 == iel)
+          val1 = (__ldg(F.indtype + n[s]) < 0 && __ldg(F.indtype + n[(s + 1) & 3]) < 0 && in2 != iel)
+                     ? 1.0 : 0.0;
+        if (in2 == iel)
+          val2 = (__ldg(F.indtype + n[s + 2]) < 0 && __ldg(F.indtype + n[(s + 3) & 3]) < 0 &&
+                  in1 != iel) ? 1.0 : 0.0;
+#pragma unroll
+        for (int e2 = 0; e2 < 2; e2++) {
+          const int is = e2 == 0 ? ((s + 3) & 3) : (s + 1);
+          FaceQ f;
+          if (is == 0) {
+            f.du = s_f0[0][t];
+            f.dv = s_f0[1][t];
+            f.lu = s_f0[2][t];
+            f.lx = s_f0[3][t];
+            f.uh = s_f0[4][t];
+            f.vh = s_f0[5][t];
+            f.xh = s_f0[6][t];
+            f.yh = s_f0[7][t];
+            f.w1 = s_f0[8][t];
+          } else if (is == 2) {
+            const int o = nb[2] - iel;
+            if ((o == 1 || o == -1) && fc_of(fcp, 2) == 0) {
+              const int q = t + o;
+              f.du = negF(s_f0[0][q]);
+              f.dv = negF(s_f0[1][q]);
+              f.lu = s_f0[2][q];
+              f.lx = s_f0[3][q];
+              f.uh = negF(s_f0[4][q]);
+              f.vh = negF(s_f0[5][q]);
+              f.xh = negF(s_f0[6][q]);
+              f.yh = negF(s_f0[7][q]);
+              f.w1 = s_f0[8][q];
+            } else {
+              f = face_q(u[3] - u[2], v[3] - v[2], x[3] - x[2], y[3] - y[2], zc);
+            }
+          } else {
+            const int o = is == 1 ? 0 : 4;
+            f = face_q(s_fd[o + 2][t], s_fd[o + 3][t], s_fd[o][t], s_fd[o + 1][t], zc);
+          }
+          // neighbour faces: edge 1 uses MOD(ielfc,4)+1 / MOD(ielfc+2,4)+1,
+          // edge 2 the other pair (hydro_kn_edgeviscosity.f90:117-151)
+          const int ins1 = e2 == 0 ? ((f1 + 1) & 3) : ((f1 + 3) & 3);
+          const int ins2 = e2 == 0 ? ((f2 + 3) & 3) : ((f2 + 1) & 3);
+          double r1 = val1, r2 = val2;
+#pragma unroll
+          for (int k = 0; k < 2; k++) {
+            const int inb = k == 0 ? in1 : in2;
+            const int ins = k == 0 ? ins1 : ins2;
+            if (inb == iel) continue;
+            double ddx, ddy, ddu, ddv;
+            const int o = inb - iel;
+            if ((o == 1 || o == -1) && (ins & 1)) {
+              const int q = t + o, c = ins == 1 ? 0 : 4;
+              ddx = s_fd[c][q];
+              ddy = s_fd[c + 1][q];
+              ddu = s_fd[c + 2][q];
+              ddv = s_fd[c + 3][q];
+            } else {
+              const int4 m = __ldg(F.ielnd + inb);
+              const int mm[4] = {m.x, m.y, m.z, m.w};
+              const int a = mm[ins], b = mm[(ins + 1) & 3];
+              ddx = F.ndx[b] - F.ndx[a];
+              ddy = F.ndy[b] - F.ndy[a];
+              ddu = F.ndu[b] - F.ndu[a];
+              ddv = F.ndv[b] - F.ndv[a];
+            }
+            const double r = nb_ratio(f, ddx, ddy, ddu, ddv, zc);
+            if (k == 0) r1 = r;
+            else r2 = r;
+          }
+          // limiter and edge coefficient (hydro_kn_edgeviscosity.f90:185-214)
+          const int ins = nb[is];
+          double w1 = C.cvisc1 * SQRT(half(cs2i + F.cs2[ins]));
+          double w2 = minF(minF(minF(half(r1 + r2), twice(r1)), twice(r2)), 1.0);
+          w2 = maxF(0.0, w2);
+          const double edv = half(1.0 - w2) * (rho0 + F.rho[ins]) * (w1 + C.cvisc2 * f.lu);
+          vmax = maxF_nn(vmax, edv * f.lu);  // never negative
+          // edge force (hydro_kn_edgeviscosity.f90:219-282): the reference
+          // normalises the midpoint-to-centroid vector c, orients it by the
+          // sign of its product with the face vector and scales it back by
+          // |c|: (exh, eyh) = -+(cy, -cx), the sign bit of w33 = cy*xh -
+          // cx*yh choosing; |c| only enters the cut test
+          const double cx = is == 0 ? ga3 : (is == 1 ? negF(ga1) : (is == 2 ? negF(ga3) : ga1));
+          const double cy = is == 0 ? gb3 : (is == 1 ? negF(gb1) : (is == 2 ? negF(gb3) : gb1));
+          const double w33 = cy * f.xh - cx * f.yh;
+          const long long sb = bits64(w33) & (long long)0x8000000000000000ull;
+          const double exh = from_bits64(bits64(cy) ^ (long long)0x8000000000000000ull ^ sb);
+          const double eyh = from_bits64(bits64(cx) ^ sb);
+          const double w7sq = (is & 1) ? c1sq : c3sq;
+          const double w6b = f.du * exh + f.dv * eyh;
+          const double d = edv * DIV(w6b, maxF_nn(f.lu, zc));
+          edx[is] = f.du * d;
+          edy[is] = f.dv * d;
+          if (le_nn(f.lu, zc) || geF(zc, w6b) || le_nn(w7sq, zc * zc) || le_nn(f.lx, zc)) {
+            edx[is] = 0.0;
+            edy[is] = 0.0;
+          }
+        }
+      }
+      visc = vmax * DIV(2.0, maxF(rho0, zc));
+      F.cnviscx[iel] = make_d4(edx[0] - edx[3], edx[1] - edx[0], edx[2] - edx[1], edx[3] - edx[2]);
+      F.cnviscy[iel] = make_d4(edy[0] - edy[3], edy[1] - edy[0], edy[2] - edy[1], edy[3] - edy[2]);
+      F.visc[iel] = visc;
+    } else {
+      visc = F.visc[iel];
+    }
+    getdt_tail(F, C, iel, x, y, u, v, visc, cflv, cfli, divv, divi);
+  }
+  getdt_finish<BS>(F, C, S, cflv, cfli, divv, divi);
+}
+
+template <int BS>
+constexpr int getdt_elements_per_block() { return BS - 2; }
+#else
+
+template <int BS>
+__global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg C) {
+  DevStep* S = F.step;
+  if (halted(S)) return;
+  if (S->stop_next) {            // bl_run: the previous step reached time_end
+    if (blockIdx.x == 0 && threadIdx.x == 0) S->halted = 1;
+    return;
+  }
+  const int iel = blockIdx.x * BS + threadIdx.x;
+  double cflv = HUGE_VAL;        // sentinel above HUGE(1.0)
+  int cfli = 0x7fffffff;
+  double divv = DBL_MIN;         // TINY(1.0)
+  int divi = -1;
+  if (iel < F.nel) {
+    const int4 nd = __ldg(F.ielnd + iel);
+    const int n[4] = {nd.x, nd.y, nd.z, nd.w};
+    double x[4], y[4], u[4], v[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      x[j] = F.ndx[n[j]];
+      y[j] = F.ndy[n[j]];
+      u[j] = F.ndu[n[j]];
+      v[j] = F.ndv[n[j]];
+    }
+    const double zc = C.zerocut;
+    const double rho0 = F.rho[iel];
+    double visc = 0.0;
+    double qx[4] = {0.0, 0.0, 0.0, 0.0}, qy[4] = {0.0, 0.0, 0.0, 0.0};
+    if (!C.ztq) {
+      // hydro_kn_initeviscosity / limiteviscosity / geteviscosity
+      // (hydro_kn_edgeviscosity.f90:30-282), evaluated face by face: every
+      // quantity of a face -- its differences (face j runs corner j ->
+      // j+1), lengths, normalised vectors, limiter ratios, edge coefficient
+      // and edge force -- is formed and consumed before the next face, which
+      // keeps the live state to the element's corners and the four edge
+      // forces.  The faces of side s (neighbours across faces s and s+2)
+      // are (s+3)&3 and s+1, in the reference's order 3, 1, 0, 2.
+      const int4 ee = __ldg(F.ielel + iel);
+      const int nb[4] = {ee.x, ee.y, ee.z, ee.w};
+      const int fcp = __ldg(F.ielfc + iel);
+      const double cs2i = F.cs2[iel];
+      const double xc = quarter(x[0] + x[1] + x[2] + x[3]);
+      const double yc = quarter(y[0] + y[1] + y[2] + y[3]);
+      double edx[4], edy[4];
+#pragma unroll
+      for (int s = 0; s < 2; s++) {
+        const int in1 = nb[s], in2 = nb[s + 2];
+        const int f1 = fc_of(fcp, s), f2 = fc_of(fcp, s + 2);
+        // boundary rule (hydro_kn_edgeviscosity.f90:154-183): a ratio across
+        // a boundary face is 1 between two boundary nodes facing an
+        // interior neighbour, 0 otherwise
+        double val1 = 0.0, val2 = 0.0;
+        if (in1 == iel)
+          val1 = (__ldg(F.indtype + n[s]) < 0 && __ldg(F.indtype + n[(s + 1) & 3]) < 0 && in2 != iel)
+                     ? 1.0 : 0.0;
+        if (in2 == iel)
+          val2 = (__ldg(F.indtype + n[s + 2]) < 0 && __ldg(F.indtype + n[(s + 3) & 3]) < 0 &&
+                  in1 != iel) ? 1.0 : 0.0;
+#pragma unroll
+        for (int e2 = 0; e2 < 2; e2++) {
+          const int is = e2 == 0 ? ((s + 3) & 3) : (s + 1);
+          const int jn = (is + 1) & 3;
+          double w1 = u[jn] - u[is], w2 = v[jn] - v[is];
+          double w3 = x[jn] - x[is], w4 = y[jn] - y[is];
+          const double du = w1, dv = w2;
+          double den = SQRT(w1 * w1 + w2 * w2);
+          const double lu = den;
+          den = DIV(1.0, maxF_nn(den, zc));
+          const double uhat = w1 * den, vhat = w2 * den;
+          den = SQRT(w3 * w3 + w4 * w4);
+          const double lx = den;
+          den = DIV(1.0, maxF_nn(den, zc));
+          const double xh = w3 * den, yh = w4 * den;
+          den = w3 * xh + w4 * yh;
+          w1 = DIV(w1 * uhat + w2 * vhat, signF(maxF_nn(absF(den), zc), den));
+          w1 = DIV(1.0, signF(maxF_nn(absF(w1), zc), w1));
+          // neighbour faces: edge 1 uses MOD(ielfc,4)+1 / MOD(ielfc+2,4)+1,
+          // edge 2 the other pair (hydro_kn_edgeviscosity.f90:117-151)
+          const int ins1 = e2 == 0 ? ((f1 + 1) & 3) : ((f1 + 3) & 3);
+          const int ins2 = e2 == 0 ? ((f2 + 3) & 3) : ((f2 + 1) & 3);
+          double r1 = val1, r2 = val2;
+          if (in1 != iel) {
+            const int4 m = __ldg(F.ielnd + in1);
+            const int mm[4] = {m.x, m.y, m.z, m.w};
+            const int a = mm[ins1], b = mm[(ins1 + 1) & 3];
+            double ddx = F.ndx[b] - F.ndx[a], ddy = F.ndy[b] - F.ndy[a];
+            double ddu = F.ndu[b] - F.ndu[a], ddv = F.ndv[b] - F.ndv[a];
+            double dn = ddx * xh + ddy * yh;
+            double q = DIV(ddu * uhat + ddv * vhat, signF(maxF_nn(absF(dn), zc), dn));
+            r1 = q * w1;
+          }
+          if (in2 != iel) {
+            const int4 m = __ldg(F.ielnd + in2);
+            const int mm[4] = {m.x, m.y, m.z, m.w};
+            const int a = mm[ins2], b = mm[(ins2 + 1) & 3];
+            double ddx = F.ndx[b] - F.ndx[a], ddy = F.ndy[b] - F.ndy[a];
+            double ddu = F.ndu[b] - F.ndu[a], ddv = F.ndv[b] - F.ndv[a];
+            double dn = ddx * xh + ddy * yh;
+            double q = DIV(ddu * uhat + ddv * vhat, signF(maxF_nn(absF(dn), zc), dn));
+            r2 = q * w1;
+          }
+          // limiter and edge coefficient (hydro_kn_edgeviscosity.f90:185-214)
+          const int ins = nb[is];
+          w1 = C.cvisc1 * SQRT(half(cs2i + F.cs2[ins]));
+          w2 = r1;
+          w3 = r2;
+          w2 = minF(minF(minF(half(w2 + w3), twice(w2)), twice(w3)), 1.0);
+          w2 = maxF(0.0, w2);
+          w4 = lu;
+          w3 = half(1.0 - w2) * (rho0 + F.rho[ins]) * (w1 + C.cvisc2 * w4);
+          const double edv = w3;
+          w4 = DIV(twice(w4), maxF(rho0, zc));
+          visc = maxF_nn(visc, w3 * w4);  // visc stays +0 or positive
+          // edge force (hydro_kn_edgeviscosity.f90:219-282)
+          {
+            const double m3 = half(x[is] + x[jn]);
+            const double m6 = half(y[is] + y[jn]);
+            const double w7 = SQRT((xc - m3) * (xc - m3) + (yc - m6) * (yc - m6));
+            const double w8 = lx;  // SQRT(w1*w1+w4*w4) of the same face difference
+            double d = DIV(1.0, w7);
+            double exh = (yc - m6) * d, eyh = (m3 - xc) * d;
+            // w1*(1/w8), w4*(1/w8): the limiter's normalised face vector
+            // whenever w8 > zerocut; otherwise the edge is cut below
+            const double w33 = exh * xh + eyh * yh;
+            d = -(signF(1.0, w33) * w7);
+            exh = exh * d;
+            eyh = eyh * d;
+            const double w5 = lu;
+            const double w6b = du * exh + dv * eyh;
+            d = DIV(w6b, maxF_nn(w5, zc));
+            edx[is] = edv * du * d;
+            edy[is] = edv * dv * d;
+            if (le_nn(w5, zc) || geF(zc, w6b) || le_nn(w7, zc) || le_nn(w8, zc)) {
+              edx[is] = 0.0;
+              edy[is] = 0.0;
+            }
+          }
+        }
+      }
+      qx[0] = edx[0] - edx[3];
+      qx[1] = edx[1] - edx[0];
+      qx[2] = edx[2] - edx[1];
+      qx[3] = edx[3] - edx[2];
+      qy[0] = edy[0] - edy[3];
+      qy[1] = edy[1] - edy[0];
+      qy[2] = edy[2] - edy[1];
+      qy[3] = edy[3] - edy[2];
+      F.cnviscx[iel] = make_d4(qx[0], qx[1], qx[2], qx[3]);
+      F.cnviscy[iel] = make_d4(qy[0], qy[1], qy[2], qy[3]);
+      F.visc[iel] = visc;
+    } else {
+      visc = F.visc[iel];
+    }
+    getdt_tail(F, C, iel, x, y, u, v, visc, cflv, cfli, divv, divi);
+  }
+  getdt_finish<BS>(F, C, S, cflv, cfli, divv, divi);
+}
+
+template <int BS>
+constexpr int getdt_elements_per_block() { return BS; }
+#endif
 
 // ================================================================ k_lag_force
 
@@ -1136,7 +1349,10 @@ static constexpr int BS_DT = 128;
 static constexpr int BS_EL = 128;
 static constexpr int BS_ND = 256;
 
-int getdt_blocks(int nel) { return (nel + BS_DT - 1) / BS_DT; }
+int getdt_blocks(int nel) {
+  constexpr int E = getdt_elements_per_block<BS_DT>();
+  return (nel + E - 1) / E;
+}
 
 void launch_getdt(const DevFields& F, const DevCfg& C, cudaStream_t s) {
   k_getdt<BS_DT><<<getdt_blocks(F.nel), BS_DT, 0, s>>>(F, C);
