@@ -740,7 +740,11 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
   int cfli = 0x7fffffff;
   double divv = DBL_MIN;         // TINY(1.0)
   int divi = -1;
-  __shared__ double s_f0[9][BS];  // face 0: du dv lu lx uh vh xh yh w1
+  // face 0: du dv lu lx uh vh xh yh w1, then the edge coefficient's two
+  // factors that do not depend on the side the face is seen from,
+  // cvisc1*sqrt((cs2 + cs2')/2) + cvisc2*|du| and rho + rho' (the same sums
+  // with the operands swapped, which IEEE addition does not change)
+  __shared__ double s_f0[11][BS];
   __shared__ double s_fd[8][BS];  // faces 1, 3: dx dy du dv each
   const double zc = C.zerocut;
   int n[4] = {0, 0, 0, 0};
@@ -771,6 +775,9 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
       s_f0[6][t] = f0.xh;
       s_f0[7][t] = f0.yh;
       s_f0[8][t] = f0.w1;
+      const int nb0 = __ldg(F.ielel + iel).x;
+      s_f0[9][t] = C.cvisc1 * SQRT(half(F.cs2[iel] + F.cs2[nb0])) + C.cvisc2 * f0.lu;
+      s_f0[10][t] = F.rho[iel] + F.rho[nb0];
       s_fd[0][t] = x[2] - x[1];
       s_fd[1][t] = y[2] - y[1];
       s_fd[2][t] = u[2] - u[1];
@@ -819,7 +826,9 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
         for (int e2 = 0; e2 < 2; e2++) {
           const int is = e2 == 0 ? ((s + 3) & 3) : (s + 1);
           FaceQ f;
+          int qf = -1;  // thread whose face-0 coefficient factors apply
           if (is == 0) {
+            qf = t;
             f.du = s_f0[0][t];
             f.dv = s_f0[1][t];
             f.lu = s_f0[2][t];
@@ -833,6 +842,7 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
             const int o = nb[2] - iel;
             if ((o == 1 || o == -1) && fc_of(fcp, 2) == 0) {
               const int q = t + o;
+              qf = q;
               f.du = negF(s_f0[0][q]);
               f.dv = negF(s_f0[1][q]);
               f.lu = s_f0[2][q];
@@ -881,11 +891,18 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
             else r2 = r;
           }
           // limiter and edge coefficient (hydro_kn_edgeviscosity.f90:185-214)
-          const int ins = nb[is];
-          double w1 = C.cvisc1 * SQRT(half(cs2i + F.cs2[ins]));
+          double cq, rs;
+          if (qf >= 0) {
+            cq = s_f0[9][qf];
+            rs = s_f0[10][qf];
+          } else {
+            const int ins = nb[is];
+            cq = C.cvisc1 * SQRT(half(cs2i + F.cs2[ins])) + C.cvisc2 * f.lu;
+            rs = rho0 + F.rho[ins];
+          }
           double w2 = minF(minF(minF(half(r1 + r2), twice(r1)), twice(r2)), 1.0);
           w2 = maxF(0.0, w2);
-          const double edv = half(1.0 - w2) * (rho0 + F.rho[ins]) * (w1 + C.cvisc2 * f.lu);
+          const double edv = half(1.0 - w2) * rs * cq;
           vmax = maxF_nn(vmax, edv * f.lu);  // never negative
           // edge force (hydro_kn_edgeviscosity.f90:219-282): the reference
           // normalises the midpoint-to-centroid vector c, orients it by the
