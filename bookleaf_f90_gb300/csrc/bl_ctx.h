@@ -22,6 +22,9 @@ struct bl_ctx {
   bl::Launchers L{};
   std::vector<void*> bufs;
   bl::DevStep* hstep = nullptr;  // pinned mirror of F.step
+  // true while *hstep equals F.step on the device: set by a completed
+  // fetch of the header, cleared whenever work that may change it is queued
+  bool hstep_current = false;
   bool cs2_is_v = false;     // elcs2 currently holds cs2 + elvisc (after getdt)
   long long launches = 0;
   // bl_run

@@ -244,3 +244,32 @@ def test_time_step_kernels_advances_like_the_device_loop():
     assert not compare(pa, pb, exact=True)
     ierr, _ = sa.time_step_kernels(65)
     assert ierr != 0 and "bad argument" in sa.error.message
+
+
+def test_host_edits_of_the_timestep_take_effect():
+    """The per-call entry points skip uploading the step header when the
+    device already holds it; a host that edits the timestep between calls
+    (dt, time, nstep) must still see its edit used, as the CPU restatement
+    uses it."""
+    from oracle.oracle import Oracle
+    base = Problem.from_deck(configs.sedov(16, kappa=0.01, pmerit=0.1))
+    pg, pc = base.copy(), base.copy()
+    s = Solver(pg, fp_mode=abi.FP_EXACT)
+    o = Oracle(pc)
+    tg, tc = pg.timestep, pc.timestep
+    for n in range(8):
+        if n == 3:                 # edit between two steps
+            for t in (tg, tc):
+                t.dt = 0.5 * t.dt
+                t.time = t.time + 1e-7
+        assert s.inf_solver_getdt(tg) == o.getdt(tc) == 0
+        if n == 5:                 # edit between getdt and lagstep
+            for t in (tg, tc):
+                t.dt = 0.75 * t.dt
+        assert s.inf_solver_lagstep(tg) == o.lagstep(tc) == 0
+        if n == 6:
+            for t in (tg, tc):
+                t.nstep = t.nstep + 10
+        assert (tg.nstep, tg.dt, tg.time) == (tc.nstep, tc.dt, tc.time)
+    s.sync_to_host(0)
+    assert not compare(pg, pc, exact=True)
