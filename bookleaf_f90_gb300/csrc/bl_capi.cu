@@ -145,6 +145,56 @@ int fetch_header(bl_ctx* x, bl_error* e, const char* where) {
   return BL_SUCCESS;
 }
 
+// The per-call entry points queue their kernels and the download of the
+// step header as one replay of a graph captured on first use (again when
+// the kernels' arguments change), then wait for it: one launch instead of
+// one per kernel plus a copy, and the graph's back-to-back kernel launches.
+enum { kCallGetdt = 0, kCallLagstep = 1, kCallAlestep = 2 };
+
+void queue_call_kernels(bl_ctx* x, int which) {
+  if (which == kCallGetdt) {
+    x->L.getdt(x->F, x->C, x->stream);
+  } else if (which == kCallLagstep) {
+    x->L.lag_force(x->F, x->C, x->stream);
+    x->L.lag_accel(x->F, x->C, x->stream);
+    x->L.lag_state(x->F, x->C, x->stream);
+  } else {
+    x->L.ale(x->F, x->C, x->stream);
+  }
+}
+
+int run_call(bl_ctx* x, int which, bl_error* e, const char* where) {
+  cudaError_t r;
+  if (!x->call_exec[which] || std::memcmp(&x->call_F[which], &x->F, sizeof x->F) != 0 ||
+      std::memcmp(&x->call_C[which], &x->C, sizeof x->C) != 0) {
+    if (x->call_exec[which]) cudaGraphExecDestroy(x->call_exec[which]);
+    x->call_exec[which] = nullptr;
+    cudaGraph_t g;
+    r = cudaStreamBeginCapture(x->stream, cudaStreamCaptureModeThreadLocal);
+    if (r != cudaSuccess) return cuda_fail(e, r, where);
+    queue_call_kernels(x, which);
+    cudaMemcpyAsync(x->hstep, x->F.step, sizeof(DevStep), cudaMemcpyDeviceToHost, x->stream);
+    r = cudaStreamEndCapture(x->stream, &g);
+    if (r != cudaSuccess) return cuda_fail(e, r, where);
+    r = cudaGraphInstantiate(&x->call_exec[which], g, 0);
+    cudaGraphDestroy(g);
+    if (r != cudaSuccess) {
+      x->call_exec[which] = nullptr;
+      return cuda_fail(e, r, where);
+    }
+    x->call_F[which] = x->F;
+    x->call_C[which] = x->C;
+  }
+  r = cudaGraphLaunch(x->call_exec[which], x->stream);
+  if (r != cudaSuccess) return cuda_fail(e, r, where);
+  r = cudaStreamSynchronize(x->stream);
+  if (r != cudaSuccess) return cuda_fail(e, r, where);
+  r = cudaGetLastError();
+  if (r != cudaSuccess) return cuda_fail(e, r, where);
+  x->hstep_current = true;
+  return BL_SUCCESS;
+}
+
 int negvol_error(int code, bl_error* e) {
   set_err(e, -code, BL_HALT_SINGLE, "ERROR: negative volume in geometry_dr_getgeometry");
   return -code;
@@ -560,6 +610,8 @@ int bl_finalize(bl_ctx* x) {
   if (!x) return BL_SUCCESS;
   if (x->stream) cudaStreamSynchronize(x->stream);
   if (x->gexec) cudaGraphExecDestroy(x->gexec);
+  for (auto& g : x->call_exec)
+    if (g) cudaGraphExecDestroy(g);
   for (void* p : x->bufs) cudaFree(p);
   if (x->F.hist) cudaFree(x->F.hist);
   if (x->diag) cudaFree(x->diag);
@@ -576,9 +628,8 @@ int bl_getdt(bl_ctx* x, bl_timestep* ts, bl_error* e) {
     return BL_FAILURE;
   }
   header_from_ts(x, ts, 0);
-  x->L.getdt(x->F, x->C, x->stream);
   x->launches += bl::kLaunchesGetdt;
-  int rc = fetch_header(x, e, "bl_getdt");
+  int rc = run_call(x, kCallGetdt, e, "bl_getdt");
   if (rc != BL_SUCCESS) return rc;
   x->cs2_is_v = true;
   const DevStep& S = *x->hstep;
@@ -601,11 +652,8 @@ int bl_lagstep(bl_ctx* x, bl_timestep* ts, bl_error* e) {
     return BL_FAILURE;
   }
   header_from_ts(x, ts, 0);
-  x->L.lag_force(x->F, x->C, x->stream);
-  x->L.lag_accel(x->F, x->C, x->stream);
-  x->L.lag_state(x->F, x->C, x->stream);
   x->launches += bl::kLaunchesLagstep;
-  int rc = fetch_header(x, e, "bl_lagstep");
+  int rc = run_call(x, kCallLagstep, e, "bl_lagstep");
   if (rc != BL_SUCCESS) return rc;
   x->cs2_is_v = false;
   // time_dr_setpredictor / setcorrector leave the corrector state behind
@@ -631,9 +679,8 @@ int bl_alestep(bl_ctx* x, const bl_timestep* ts, bl_error* e) {
     return BL_FAILURE;
   }
   header_from_ts(x, ts, 0);
-  x->L.ale(x->F, x->C, x->stream);
   x->launches += bl::kLaunchesAle;
-  int rc = fetch_header(x, e, "bl_alestep");
+  int rc = run_call(x, kCallAlestep, e, "bl_alestep");
   if (rc != BL_SUCCESS) return rc;
   const DevStep& S = *x->hstep;
   if (S.negvol_ale) return negvol_error(S.negvol_ale, e);

@@ -27,6 +27,12 @@ struct bl_ctx {
   bool hstep_current = false;
   bool cs2_is_v = false;     // elcs2 currently holds cs2 + elvisc (after getdt)
   long long launches = 0;
+  // per-call entry points: one cached graph each (getdt, lagstep, alestep)
+  // of their kernels and the header download, with the kernel arguments it
+  // was captured with
+  cudaGraphExec_t call_exec[3] = {nullptr, nullptr, nullptr};
+  bl::DevFields call_F[3] = {};
+  bl::DevCfg call_C[3] = {};
   // bl_run
   cudaGraphExec_t gexec = nullptr;
   int gsteps = 0;
