@@ -77,6 +77,28 @@ static __device__ __noinline__ double dsqrt_call(double x) { return dsqrt_rn(x);
 #ifndef BL_FORCE_MINB
 #define BL_FORCE_MINB 4
 #endif
+// Minimum resident blocks per SM of the two short kernels (0: the plain
+// block-size bound).  From the same whole-run sweep: k_lag_accel with a
+// one-block bound takes 56 registers and no spills (24.8 us against 26.3 us
+// at the 40 registers of the plain bound, 913.7M against 907.8M
+// zone-cycles/s); k_lag_state is best with the plain bound (72 registers;
+// 1, 8, 12 and 16 blocks were slower or equal).
+#ifndef BL_ACCEL_MINB
+#define BL_ACCEL_MINB 1
+#endif
+#ifndef BL_STATE_MINB
+#define BL_STATE_MINB 0
+#endif
+#if BL_ACCEL_MINB > 0
+#define BL_ACCEL_BOUNDS(bs) __launch_bounds__(bs, BL_ACCEL_MINB)
+#else
+#define BL_ACCEL_BOUNDS(bs) __launch_bounds__(bs)
+#endif
+#if BL_STATE_MINB > 0
+#define BL_STATE_BOUNDS(bs) __launch_bounds__(bs, BL_STATE_MINB)
+#else
+#define BL_STATE_BOUNDS(bs) __launch_bounds__(bs)
+#endif
 
 namespace bl {
 namespace BL_NS {
@@ -1224,7 +1246,7 @@ __global__ void __launch_bounds__(BS, BL_FORCE_MINB) k_lag_force(DevFields F, De
 // ================================================================ k_lag_accel
 
 template <int BS>
-__global__ void __launch_bounds__(BS) k_lag_accel(DevFields F, DevCfg C) {
+__global__ void BL_ACCEL_BOUNDS(BS) k_lag_accel(DevFields F, DevCfg C) {
   const DevStep* S = F.step;
   if (halted(S)) return;
   const int ind = blockIdx.x * BS + threadIdx.x;
@@ -1292,7 +1314,7 @@ __global__ void __launch_bounds__(BS) k_lag_accel(DevFields F, DevCfg C) {
 // ================================================================ k_lag_state
 
 template <int BS>
-__global__ void __launch_bounds__(BS) k_lag_state(DevFields F, DevCfg C) {
+__global__ void BL_STATE_BOUNDS(BS) k_lag_state(DevFields F, DevCfg C) {
   const DevStep* S = F.step;
   if (halted(S)) return;
   const int iel = blockIdx.x * BS + threadIdx.x;
