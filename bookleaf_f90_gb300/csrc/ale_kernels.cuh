@@ -51,6 +51,26 @@ __device__ __forceinline__ double face_dv(double x1, double x2, double y1, doubl
   return quarter(a1 * b3 - a3 * b1);
 }
 
+// w7 * m with w7 = SIGN(1, w) and m >= 0, and the test w1 * w2 <= 0 of the
+// limiters.  The fast build takes the sign bit instead of the product (the
+// same in real arithmetic: opposite signs or a zero), the exact build
+// evaluates them as written.
+__device__ __forceinline__ double sign_of(double m, double w) {
+#if BL_FAST_ALGEBRA
+  return signF(m, w);
+#else
+  return signF(1.0, w) * m;
+#endif
+}
+__device__ __forceinline__ bool prod_le0(double w1, double w2) {
+#if BL_FAST_ALGEBRA
+  const long long b1 = bits64(w1), b2 = bits64(w2);
+  return (b1 ^ b2) < 0 || (b1 << 1) == 0 || (b2 << 1) == 0;
+#else
+  return geF(0.0, w1 * w2);
+#endif
+}
+
 // The limited face flux of ale_kn_fluxelvl for the pair (i1, i2=i1+2),
 // returning (fcflux(i1), fcflux(i2)) (ale_kn_advectors.f90:48-78).
 __device__ __forceinline__ void elvl_pair(int iel, int i1, const int* nb, const int* fc,
@@ -69,10 +89,9 @@ __device__ __forceinline__ void elvl_pair(int iel, int i1, const int* nb, const 
   double w1 = rv - elvar[iel2];
   double w2 = elvar[iel1] - rv;
   double w3 = absF(w1), w4 = absF(w2);
-  double w7 = signF(1.0, w2);
   double w8 = DIV(w1 * w6 * w6 + w2 * w5 * w5, w5 * w6 * (w5 + w6));
-  double grad = w7 * minF(minF(absF(w8), DIV(w3, w5)), DIV(w4, w6));
-  if (geF(0.0, w1 * w2)) grad = 0.0;
+  double grad = sign_of(minF(minF(absF(w8), DIV(w3, w5)), DIV(w4, w6)), w2);
+  if (prod_le0(w1, w2)) grad = 0.0;
   o1 = r1 * (rv + grad * (r3 - half(r1)));
   o2 = r2 * (rv - grad * (r4 - half(r2)));
   (void)iel;
@@ -90,6 +109,22 @@ __global__ void __launch_bounds__(BS) k_ale_flux(DevFields F, DevCfg C) {
   const double zc = C.zerocut;
   const int4 nd = __ldg(F.ielnd + iel);
   const int n[4] = {nd.x, nd.y, nd.z, nd.w};
+#if BL_FAST_ALGEBRA
+  // Fast build: the face's swept volume from the face vector (Dx, Dy) and
+  // the differences and sums of the mesh velocity -ubar at its ends: the
+  // reference's quarter(a1*b3 - a3*b1) of the quad (x0(j), x0(j+1),
+  // x1(j+1), x1(j)) with x1 = x0 - dt*ubar expands (exactly in real
+  // arithmetic) to dt/4 * (2 (Dy Su - Dx Sv) + dt (Du Sv - Dv Su)), which
+  // also avoids the cancellation of subtracting positions at two times.
+  double x0[4], y0[4], ub[4], vb[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    x0[j] = F.ndx[n[j]];
+    y0[j] = F.ndy[n[j]];
+    ub[j] = F.ndubar[n[j]];
+    vb[j] = F.ndvbar[n[j]];
+  }
+#else
   double x0[4], y0[4], x1[4], y1[4];
 #pragma unroll
   for (int j = 0; j < 4; j++) {
@@ -99,11 +134,20 @@ __global__ void __launch_bounds__(BS) k_ale_flux(DevFields F, DevCfg C) {
     x1[j] = x0[j] + dt * (-F.ndubar[n[j]]);
     y1[j] = y0[j] + dt * (-F.ndvbar[n[j]]);
   }
+#endif
   double fv[4], fvn[4];
 #pragma unroll
   for (int jj = 0; jj < 4; jj++) {
     const int jp = (jj + 1) & 3;
+#if BL_FAST_ALGEBRA
+    const double Dx = x0[jp] - x0[jj], Dy = y0[jp] - y0[jj];
+    const double Du = ub[jp] - ub[jj], Dv = vb[jp] - vb[jj];
+    const double Su = ub[jp] + ub[jj], Sv = vb[jp] + vb[jj];
+    const double A = Dy * Su - Dx * Sv, B = Du * Sv - Dv * Su;
+    double d = quarter(dt * fma(dt, B, twice(A)));
+#else
     double d = face_dv(x0[jj], x0[jp], y0[jj], y0[jp], x1[jp], x1[jj], y1[jp], y1[jj]);
+#endif
     fv[jj] = gtF(zc, d) ? 0.0 : d;
     double dn = -d;   // the neighbour's volume of the same face
     fvn[jj] = gtF(zc, dn) ? 0.0 : dn;
@@ -221,6 +265,41 @@ __global__ void __launch_bounds__(BS) k_ale_el(DevFields F, DevCfg C) {
       const int ii = ilfcl + 2 * (icn - 1);
       const double cdb = cndm[ii];
       double rdu = 0.0, rdv = 0.0;
+#if BL_FAST_ALGEBRA
+      // Fast build: the two branches (the corner's mass flux towards the
+      // left neighbour, cdb > 0, or from the right one, cdb < 0) are one
+      // computation with the corners and the neighbour swapped: near is the
+      // corner of the pair the limiter is centred on, far the other one,
+      // and the right branch's inner and outer differences are the left
+      // form's negated (exactly), so a single branch-free path serves both
+      // and a warp with fluxes of both signs runs it once.
+      const bool lft = gtF(cdb, 0.0);
+      if (lft || gtF(0.0, cdb)) {
+        const int nbe = lft ? iell : ielr;
+        const int lnl = lft ? (ifcl + icn) % 4 : (ifcr + icn - 2) % 4;
+        const int lnr = lft ? (ifcl - icn + 1) % 4 : (((ifcr - icn - 1) % 4) + 4) % 4;
+        const int nearc = lft ? ilndl : ilndr, farc = lft ? ilndr : ilndl;
+        const int4 m = __ldg(F.ielnd + nbe);
+        const int mm[4] = {m.x, m.y, m.z, m.w};
+        const int nbn = mm[lft ? lnl : lnr];
+        const double rd0 = ob[nearc] - half(absF(cdb));
+        const double w5 = ob[ilndl] + ob[ilndr];
+        const double w6 = cget(F.cnmass, nbe, lnl) + cget(F.cnmass, nbe, lnr);
+        const double den = w5 * w6 * (w5 + w6);
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+          const double* cvar = q == 0 ? cu : cv;
+          const double* nvar = q == 0 ? F.ndu : F.ndv;
+          const double rv = cvar[nearc];
+          const double I = cvar[farc] - rv, O = rv - nvar[nbn];
+          const double w8 = DIV(I * w6 * w6 + O * w5 * w5, den);
+          double grad = sign_of(minF(minF(absF(w8), DIV(absF(O), w6)), DIV(absF(I), w5)), I);
+          if (prod_le0(O, I)) grad = 0.0;
+          const double rd = cdb * (rv + grad * rd0);
+          if (q == 0) rdu = rd; else rdv = rd;
+        }
+      }
+#else
       if (gtF(cdb, 0.0)) {
         const int lnl = (ifcl + icn) % 4;
         const int lnr = (ifcl - icn + 1) % 4;
@@ -238,10 +317,9 @@ __global__ void __launch_bounds__(BS) k_ale_el(DevFields F, DevCfg C) {
           double w1 = rv - nvar[mm[lnl]];
           double w2 = cvar[ilndr] - rv;
           double w3 = absF(w1), w4 = absF(w2);
-          double w7 = signF(1.0, w2);
           double w8 = DIV(w2 * w6 * w6 + w1 * w5 * w5, den);
-          double grad = w7 * minF(minF(absF(w8), DIV(w3, w6)), DIV(w4, w5));
-          if (geF(0.0, w1 * w2)) grad = 0.0;
+          double grad = sign_of(minF(minF(absF(w8), DIV(w3, w6)), DIV(w4, w5)), w2);
+          if (prod_le0(w1, w2)) grad = 0.0;
           double rd = cdb * (rv + grad * rd0);
           if (q == 0) rdu = rd; else rdv = rd;
         }
@@ -263,14 +341,14 @@ __global__ void __launch_bounds__(BS) k_ale_el(DevFields F, DevCfg C) {
           double w1 = rv - cvar[ilndl];
           double w2 = nvar[mm[lnr]] - rv;
           double w3 = absF(w1), w4 = absF(w2);
-          double w7 = signF(1.0, w2);
           double w8 = DIV(w1 * w6 * w6 + w2 * w5 * w5, den);
-          double grad = -(w7 * minF(minF(absF(w8), DIV(w3, w5)), DIV(w4, w6)));
-          if (geF(0.0, w1 * w2)) grad = 0.0;
+          double grad = -sign_of(minF(minF(absF(w8), DIV(w3, w5)), DIV(w4, w6)), w2);
+          if (prod_le0(w1, w2)) grad = 0.0;
           double rd = cdb * (rv + grad * rd0);
           if (q == 0) rdu = rd; else rdv = rd;
         }
       }
+#endif
       fu[ilndl] = fu[ilndl] - rdu;
       fu[ilndr] = fu[ilndr] + rdu;
       fv[ilndl] = fv[ilndl] - rdv;
