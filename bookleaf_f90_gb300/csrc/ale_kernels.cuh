@@ -34,7 +34,7 @@ __device__ __forceinline__ bool halted_a(const DevStep* S) {
 __device__ __forceinline__ bool ale_on(const DevCfg& C, const DevStep* S) {
   if (!C.ale_zexist) return false;
   const double t = S->time;
-  return (t >= C.ale_mintime) && (t <= C.ale_maxtime);
+  return geF(t, C.ale_mintime) && geF(C.ale_maxtime, t);  // the IEEE >= on the integer pipe
 }
 
 __device__ __forceinline__ double cget(const d4* a, int iel, int j) {
