@@ -55,6 +55,12 @@ def load(build_if_missing=True):
     L.bl_time_step_kernels.argtypes = [vp, P(abi.Timestep), ct.c_int, P(ct.c_double), ct.c_int,
                                        P(abi.Error)]
     L.bl_time_step_kernels.restype = ct.c_int
+    L.bl_init_batch.argtypes = [P(vp), ct.c_int, vp, vp, vp, ct.c_int, P(abi.Error)]
+    L.bl_init_batch.restype = ct.c_int
+    L.bl_run_batch.argtypes = [vp, vp, ct.c_int, P(ct.c_int), P(ct.c_int), P(abi.Error)]
+    L.bl_run_batch.restype = ct.c_int
+    L.bl_batch_size.argtypes = [vp]
+    L.bl_batch_size.restype = ct.c_int
     L.bl_fp64_rates.restype = ct.c_int
     L.bl_shortprint.argtypes = [vp, ct.c_int, P(ct.c_double), ct.c_int, P(abi.Error)]
     L.bl_shortprint.restype = ct.c_int
@@ -70,7 +76,8 @@ def load(build_if_missing=True):
 EXPORTS = ("bl_init", "bl_finalize", "bl_getdt", "bl_lagstep", "bl_alestep", "bl_run",
            "bl_sync_to_host", "bl_sync_to_device", "bl_synchronize", "bl_stream",
            "bl_kernel_launches", "bl_version", "bl_getdt_noalloc", "bl_selftest_fp64",
-           "bl_fp64_rates", "bl_shortprint", "bl_check_sod", "bl_time_step_kernels")
+           "bl_fp64_rates", "bl_shortprint", "bl_check_sod", "bl_time_step_kernels",
+           "bl_init_batch", "bl_run_batch", "bl_batch_size")
 
 
 def fp64_rates():

@@ -1,0 +1,76 @@
+"""A batch of independent problems advanced together on the device.
+
+``BatchSolver`` registers several Problems -- each what one control file
+describes, with its own mesh, materials, time-step controls and end time --
+with bl_init_batch, and advances them with bl_run_batch: one kernel per
+phase over all the meshes, each mesh keeping its own dt and time on the
+device.  Every mesh ends as it would running alone (bit for bit in exact
+mode).  ``sync_to_host`` updates each Problem's own arrays.
+"""
+import ctypes as ct
+
+from . import abi
+from ._lib import load
+from .solver import SolverError
+
+
+class BatchSolver:
+    def __init__(self, problems, fp_mode=abi.FP_FAST):
+        self.L = load()
+        self.problems = list(problems)
+        n = len(self.problems)
+        self.error = abi.Error()
+        self._tabs = [p.pointer_table() for p in self.problems]
+        self._sizes = (abi.Sizes * n)(*[p.sizes for p in self.problems])
+        self._configs = (abi.Config * n)(*[p.config for p in self.problems])
+        self._dh = (ct.c_void_p * n)(*[ct.cast(t, ct.c_void_p) for t in self._tabs])
+        self.ctx = ct.c_void_p()
+        ierr = self.L.bl_init_batch(ct.byref(self.ctx), n, ct.cast(self._sizes, ct.c_void_p),
+                                    ct.cast(self._configs, ct.c_void_p),
+                                    ct.cast(self._dh, ct.c_void_p), int(fp_mode),
+                                    ct.byref(self.error))
+        if ierr != 0:
+            raise SolverError(ierr, self.error.iout, self.error.message)
+
+    def __len__(self):
+        return len(self.problems)
+
+    def run(self, max_steps=10**9):
+        """Advances every mesh until its end time (or an error, or max_steps
+        steps).  Returns (ierr, per-mesh status list, steps run); each
+        Problem's timestep is updated."""
+        n = len(self.problems)
+        ts = (abi.Timestep * n)(*[p.timestep for p in self.problems])
+        status = (ct.c_int * n)()
+        nsteps = ct.c_int(0)
+        ierr = self.L.bl_run_batch(self.ctx, ct.cast(ts, ct.c_void_p),
+                                   int(min(max_steps, 2**31 - 1)), status, ct.byref(nsteps),
+                                   ct.byref(self.error))
+        for p, t in zip(self.problems, ts):
+            ct.memmove(ct.addressof(p.timestep), ct.addressof(t), ct.sizeof(abi.Timestep))
+        return ierr, list(status), nsteps.value
+
+    def sync_to_host(self, fid=0):
+        return self.L.bl_sync_to_host(self.ctx, fid)
+
+    def sync_to_device(self, fid=0):
+        return self.L.bl_sync_to_device(self.ctx, fid)
+
+    @property
+    def stream(self):
+        return self.L.bl_stream(self.ctx)
+
+    @property
+    def kernel_launches(self):
+        return self.L.bl_kernel_launches(self.ctx)
+
+    def close(self):
+        if self.ctx:
+            self.L.bl_finalize(self.ctx)
+            self.ctx = ct.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

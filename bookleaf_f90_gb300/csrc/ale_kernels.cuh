@@ -99,12 +99,12 @@ __device__ __forceinline__ void elvl_pair(int iel, int i1, const int* nb, const 
 
 // ================================================================ k_ale_flux
 
-template <int BS>
+template <int BS, bool BATCH>
 __global__ void __launch_bounds__(BS) k_ale_flux(DevFields F, DevCfg C) {
-  const DevStep* S = F.step;
-  if (halted_a(S) || !ale_on(C, S)) return;
   const int iel = blockIdx.x * BS + threadIdx.x;
   if (iel >= F.nel) return;
+  DevStep* S = el_step<BATCH>(F, iel);
+  if (halted_a(S) || !ale_on(C, S)) return;
   const double dt = S->dt;
   const double zc = C.zerocut;
   const int4 nd = __ldg(F.ielnd + iel);
@@ -180,12 +180,12 @@ __global__ void __launch_bounds__(BS) k_ale_flux(DevFields F, DevCfg C) {
 
 // ================================================================ k_ale_el
 
-template <int BS>
+template <int BS, bool BATCH>
 __global__ void __launch_bounds__(BS) k_ale_el(DevFields F, DevCfg C) {
-  const DevStep* S = F.step;
-  if (halted_a(S) || !ale_on(C, S)) return;
   const int iel = blockIdx.x * BS + threadIdx.x;
   if (iel >= F.nel) return;
+  DevStep* S = el_step<BATCH>(F, iel);
+  if (halted_a(S) || !ale_on(C, S)) return;
   const double zc = C.zerocut;
   const int4 ee = __ldg(F.ielel + iel);
   const int nb[4] = {ee.x, ee.y, ee.z, ee.w};
@@ -362,12 +362,12 @@ __global__ void __launch_bounds__(BS) k_ale_el(DevFields F, DevCfg C) {
 
 // ================================================================ k_ale_nd
 
-template <int BS>
+template <int BS, bool BATCH>
 __global__ void __launch_bounds__(BS) k_ale_nd(DevFields F, DevCfg C) {
-  const DevStep* S = F.step;
-  if (halted_a(S) || !ale_on(C, S)) return;
   const int ind = blockIdx.x * BS + threadIdx.x;
   if (ind >= F.nnd) return;
+  const DevStep* S = nd_step<BATCH>(F, ind);
+  if (halted_a(S) || !ale_on(C, S)) return;
   const double dt = S->dt;
   // calcbasisnd + massbasisnd in element-major (ielsort2) order
   double v0 = 0.0, m0 = 0.0;
@@ -404,12 +404,12 @@ __global__ void __launch_bounds__(BS) k_ale_nd(DevFields F, DevCfg C) {
 
 // ================================================================ k_ale_update
 
-template <int BS>
+template <int BS, bool BATCH>
 __global__ void __launch_bounds__(BS) k_ale_update(DevFields F, DevCfg C) {
-  const DevStep* S = F.step;
-  if (halted_a(S) || !ale_on(C, S)) return;
   const int iel = blockIdx.x * BS + threadIdx.x;
   if (iel >= F.nel) return;
+  DevStep* S = el_step<BATCH>(F, iel);
+  if (halted_a(S) || !ale_on(C, S)) return;
   const int4 ee = __ldg(F.ielel + iel);
   const int nb[4] = {ee.x, ee.y, ee.z, ee.w};
   const int fcp = __ldg(F.ielfc + iel);
@@ -444,7 +444,7 @@ __global__ void __launch_bounds__(BS) k_ale_update(DevFields F, DevCfg C) {
     y[j] = F.ndy[n[j]];
   }
   Iso g = getiso(x, y);
-  if (gtF(0.0, g.vol)) atomicMax(&F.step->negvol_ale, iel + 1);
+  if (gtF(0.0, g.vol)) atomicMax(&S->negvol_ale, iel + 1 - el_base<BATCH>(F, iel));
   const double rho = DIV(m1, g.vol);
   double p, cs2;
   eos_pc(C, __ldg(F.ielmat + iel), rho, e, p, cs2);
@@ -482,12 +482,19 @@ __global__ void __launch_bounds__(BS) k_ale_update(DevFields F, DevCfg C) {
 static constexpr int BS_A = 128;
 static constexpr int BS_AN = 256;
 
-void launch_ale(const DevFields& F, const DevCfg& C, cudaStream_t s) {
+template <bool BATCH>
+void launch_ale_t(const DevFields& F, const DevCfg& C, cudaStream_t s) {
   const int ge = (F.nel + BS_A - 1) / BS_A;
-  k_ale_flux<BS_A><<<ge, BS_A, 0, s>>>(F, C);
-  k_ale_el<BS_A><<<ge, BS_A, 0, s>>>(F, C);
-  k_ale_nd<BS_AN><<<(F.nnd + BS_AN - 1) / BS_AN, BS_AN, 0, s>>>(F, C);
-  k_ale_update<BS_A><<<ge, BS_A, 0, s>>>(F, C);
+  k_ale_flux<BS_A, BATCH><<<ge, BS_A, 0, s>>>(F, C);
+  k_ale_el<BS_A, BATCH><<<ge, BS_A, 0, s>>>(F, C);
+  k_ale_nd<BS_AN, BATCH><<<(F.nnd + BS_AN - 1) / BS_AN, BS_AN, 0, s>>>(F, C);
+  k_ale_update<BS_A, BATCH><<<ge, BS_A, 0, s>>>(F, C);
+}
+void launch_ale(const DevFields& F, const DevCfg& C, cudaStream_t s) {
+  launch_ale_t<false>(F, C, s);
+}
+void launch_ale_batch(const DevFields& F, const DevCfg& C, cudaStream_t s) {
+  launch_ale_t<true>(F, C, s);
 }
 
 }  // namespace BL_NS

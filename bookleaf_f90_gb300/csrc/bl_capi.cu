@@ -25,12 +25,22 @@ using bl::d4;
 
 namespace {
 
-const bl::Launchers kFast = {bl::fast::getdt_blocks, bl::fast::launch_getdt,
-                             bl::fast::launch_lag_force, bl::fast::launch_lag_accel,
-                             bl::fast::launch_lag_state, bl::fast::launch_ale};
-const bl::Launchers kExact = {bl::exact::getdt_blocks, bl::exact::launch_getdt,
-                              bl::exact::launch_lag_force, bl::exact::launch_lag_accel,
-                              bl::exact::launch_lag_state, bl::exact::launch_ale};
+const bl::Launchers kFast = {bl::fast::getdt_blocks,          bl::fast::launch_getdt,
+                             bl::fast::launch_lag_force,       bl::fast::launch_lag_accel,
+                             bl::fast::launch_lag_state,       bl::fast::launch_ale,
+                             bl::fast::launch_getdt_batch,     bl::fast::launch_lag_force_batch,
+                             bl::fast::launch_lag_accel_batch, bl::fast::launch_lag_state_batch,
+                             bl::fast::launch_ale_batch};
+const bl::Launchers kExact = {bl::exact::getdt_blocks,          bl::exact::launch_getdt,
+                              bl::exact::launch_lag_force,       bl::exact::launch_lag_accel,
+                              bl::exact::launch_lag_state,       bl::exact::launch_ale,
+                              bl::exact::launch_getdt_batch,     bl::exact::launch_lag_force_batch,
+                              bl::exact::launch_lag_accel_batch, bl::exact::launch_lag_state_batch,
+                              bl::exact::launch_ale_batch};
+
+// batches (defined with bl_init_batch below)
+void batch_copy(bl_ctx* x, int id, bool to_mesh);
+
 
 void set_err(bl_error* e, int ierr, int iout, const char* msg) {
   if (!e) return;
@@ -45,6 +55,16 @@ int cuda_fail(bl_error* e, cudaError_t r, const char* where) {
   std::snprintf(msg, sizeof msg, "ERROR: CUDA %s in %s", cudaGetErrorString(r), where);
   set_err(e, BL_FAILURE, BL_HALT_ALL, msg);
   return BL_FAILURE;
+}
+
+// The single-mesh solver entry points and diagnostics refuse a batch
+// context (its meshes each have their own time step: bl_run_batch).
+bool reject_batch(bl_ctx* x, bl_error* e, const char* where) {
+  if (!x || x->ninst == 0) return false;
+  char msg[BL_SLEN + 1];
+  std::snprintf(msg, sizeof msg, "ERROR: %s on a batch context (use bl_run_batch)", where);
+  set_err(e, BL_FAILURE, BL_HALT_ALL, msg);
+  return true;
 }
 
 template <class T>
@@ -206,8 +226,21 @@ extern "C" {
 
 const char* bl_version(void) { return "bookleaf_gb300 1.0 (sm_103a)"; }
 
-int bl_init(bl_ctx** out, const bl_sizes* sizes, const bl_config* config, void* const* dh,
-            int fp_mode, bl_error* error) {
+}  // extern "C"
+
+namespace {
+
+// Region and material tables of a batch, concatenated over its meshes (a
+// batch may hold more of either than one control file's bound).
+struct Tables {
+  std::vector<double> kap, pm;
+  std::vector<int> zd, zm;
+  std::vector<int> et;        // [nmat+1]
+  std::vector<double> ep;     // [(nmat+1)*6]
+};
+
+int init_impl(bl_ctx** out, const bl_sizes* sizes, const bl_config* config, void* const* dh,
+              int fp_mode, bl_error* error, const Tables* T) {
   set_err(error, BL_SUCCESS, BL_HALT_SINGLE, "");
   if (!out || !sizes || !config || !dh) {
     set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init: null argument");
@@ -222,8 +255,8 @@ int bl_init(bl_ctx** out, const bl_sizes* sizes, const bl_config* config, void* 
   }
   const bl_sizes& s = *sizes;
   const bl_config& c = *config;
-  if (s.nel < 1 || s.nnd < 4 || s.nreg < 1 || s.nreg > BL_MAXREG || s.nmat < 1 ||
-      s.nmat > BL_MAXMAT || s.ncp < 0 || s.nmx < 0) {
+  if (s.nel < 1 || s.nnd < 4 || s.nreg < 1 || (!T && s.nreg > BL_MAXREG) || s.nmat < 1 ||
+      (!T && s.nmat > BL_MAXMAT) || s.ncp < 0 || s.nmx < 0) {
     set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init: sizes out of range");
     return BL_FAILURE;
   }
@@ -558,14 +591,29 @@ int bl_init(bl_ctx** out, const bl_sizes* sizes, const bl_config* config, void* 
     C.ale_zeul = c.ale_zeul;
     C.adv_type = c.ale_adv_type;
     const int nr = s.nreg, nm = s.nmat + 1;
-    std::vector<double> kap(c.kappareg, c.kappareg + nr), pm(c.pmeritreg, c.pmeritreg + nr);
-    std::vector<int> zd(c.zdtnotreg, c.zdtnotreg + nr), zm(c.zmidlength, c.zmidlength + nr);
-    std::vector<int> et(c.eos_type, c.eos_type + nm);
-    std::vector<double> ep(6L * nm), gm1(nm), ggm1(nm);
+    std::vector<double> kap, pm, ep;
+    std::vector<int> zd, zm, et;
+    if (T) {
+      kap = T->kap;
+      pm = T->pm;
+      zd = T->zd;
+      zm = T->zm;
+      et = T->et;
+      ep = T->ep;
+    } else {
+      kap.assign(c.kappareg, c.kappareg + nr);
+      pm.assign(c.pmeritreg, c.pmeritreg + nr);
+      zd.assign(c.zdtnotreg, c.zdtnotreg + nr);
+      zm.assign(c.zmidlength, c.zmidlength + nr);
+      et.assign(c.eos_type, c.eos_type + nm);
+      ep.resize(6L * nm);
+      for (int m = 0; m < nm; m++)
+        for (int k = 0; k < 6; k++) ep[6 * m + k] = c.eos_param[m][k];
+    }
+    std::vector<double> gm1(nm), ggm1(nm);
     for (int m = 0; m < nm; m++) {
-      for (int k = 0; k < 6; k++) ep[6 * m + k] = c.eos_param[m][k];
-      gm1[m] = c.eos_param[m][0] - 1.0;
-      ggm1[m] = c.eos_param[m][0] * (c.eos_param[m][0] - 1.0);
+      gm1[m] = ep[6 * m] - 1.0;
+      ggm1[m] = ep[6 * m] * (ep[6 * m] - 1.0);
     }
     double* d_kap = dalloc<double>(x, nr, st);
     double* d_pm = dalloc<double>(x, nr, st);
@@ -606,12 +654,23 @@ fail:
   return cuda_fail(error, st == cudaSuccess ? cudaErrorMemoryAllocation : st, "bl_init");
 }
 
+}  // namespace
+
+extern "C" {
+
+int bl_init(bl_ctx** out, const bl_sizes* sizes, const bl_config* config, void* const* dh,
+            int fp_mode, bl_error* error) {
+  return init_impl(out, sizes, config, dh, fp_mode, error, nullptr);
+}
+
 int bl_finalize(bl_ctx* x) {
   if (!x) return BL_SUCCESS;
   if (x->stream) cudaStreamSynchronize(x->stream);
   if (x->gexec) cudaGraphExecDestroy(x->gexec);
+  if (x->bexec) cudaGraphExecDestroy(x->bexec);
   for (auto& g : x->call_exec)
     if (g) cudaGraphExecDestroy(g);
+  if (x->hsteps) cudaFreeHost(x->hsteps);
   for (void* p : x->bufs) cudaFree(p);
   if (x->F.hist) cudaFree(x->F.hist);
   if (x->diag) cudaFree(x->diag);
@@ -623,6 +682,7 @@ int bl_finalize(bl_ctx* x) {
 
 int bl_getdt(bl_ctx* x, bl_timestep* ts, bl_error* e) {
   set_err(e, BL_SUCCESS, BL_HALT_SINGLE, "");
+  if (reject_batch(x, e, "bl_getdt")) return BL_FAILURE;
   if (!x || !ts) {
     set_err(e, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_getdt: null argument");
     return BL_FAILURE;
@@ -647,6 +707,7 @@ int bl_getdt(bl_ctx* x, bl_timestep* ts, bl_error* e) {
 
 int bl_lagstep(bl_ctx* x, bl_timestep* ts, bl_error* e) {
   set_err(e, BL_SUCCESS, BL_HALT_SINGLE, "");
+  if (reject_batch(x, e, "bl_lagstep")) return BL_FAILURE;
   if (!x || !ts) {
     set_err(e, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_lagstep: null argument");
     return BL_FAILURE;
@@ -667,6 +728,7 @@ int bl_lagstep(bl_ctx* x, bl_timestep* ts, bl_error* e) {
 
 int bl_alestep(bl_ctx* x, const bl_timestep* ts, bl_error* e) {
   set_err(e, BL_SUCCESS, BL_HALT_SINGLE, "");
+  if (reject_batch(x, e, "bl_alestep")) return BL_FAILURE;
   if (!x || !ts) {
     set_err(e, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_alestep: null argument");
     return BL_FAILURE;
@@ -690,6 +752,7 @@ int bl_alestep(bl_ctx* x, const bl_timestep* ts, bl_error* e) {
 int bl_run(bl_ctx* x, bl_timestep* ts, int max_steps, bl_step_record* history, int* nsteps,
            bl_error* e) {
   set_err(e, BL_SUCCESS, BL_HALT_SINGLE, "");
+  if (reject_batch(x, e, "bl_run")) return BL_FAILURE;
   if (nsteps) *nsteps = 0;
   if (!x || !ts || max_steps < 0) {
     set_err(e, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_run: bad argument");
@@ -812,6 +875,7 @@ int bl_run(bl_ctx* x, bl_timestep* ts, int max_steps, bl_step_record* history, i
 // events once the last one has completed.
 int bl_time_step_kernels(bl_ctx* x, bl_timestep* ts, int nstep, double* ms, int n, bl_error* e) {
   set_err(e, BL_SUCCESS, BL_HALT_SINGLE, "");
+  if (reject_batch(x, e, "bl_time_step_kernels")) return BL_FAILURE;
   constexpr int kMaxSteps = 64;
   if (!x || !ts || !ms || n < 4 || nstep < 1 || nstep > kMaxSteps) {
     set_err(e, BL_FAILURE, BL_HALT_ALL,
@@ -974,9 +1038,11 @@ int bl_sync_to_host(bl_ctx* x, int id) {
       for (int m = 0; m < x->s.nmx; m++)
         for (int k = 0; k < imxncp[m]; k++) h[imxfcp[m] - 1 + k] = el[imxel[m] - 1];
     }
+    if (x->ninst > 0) batch_copy(x, id, true);
     return BL_SUCCESS;
   }
   r = cudaMemcpy(x->host[id], dev_ptr(x, id), n * sizeof(double), cudaMemcpyDeviceToHost);
+  if (r == cudaSuccess && x->ninst > 0) batch_copy(x, id, true);
   return r == cudaSuccess ? BL_SUCCESS : BL_FAILURE;
 }
 
@@ -994,6 +1060,7 @@ int bl_sync_to_device(bl_ctx* x, int id) {
   size_t n = field_count(x, id, kind);
   if (kind < 0 || kind == 4) return BL_SUCCESS;
   void* d = dev_ptr(x, id);
+  if (x->ninst > 0) batch_copy(x, id, false);
   cudaError_t r = cudaMemcpy(d, x->host[id], n * sizeof(double), cudaMemcpyHostToDevice);
   if (id == BL_ELCS2 && r == cudaSuccess)  // keep both copies of elcs2 equal
     r = cudaMemcpy(x->cs2_is_v ? x->F.cs2 : x->F.cs2v, x->host[id], n * sizeof(double),
@@ -1017,5 +1084,396 @@ int bl_abi_sizes(int* out, int n) {
   for (int i = 0; i < n && i < 5; i++) out[i] = v[i];
   return 5;
 }
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ batches
+// Several independent meshes (each one control file's problem) advanced
+// together: one kernel per phase over all of them, each mesh with its own
+// step header (dt, time, end test, errors).  The host arrays of the meshes
+// are concatenated into one disconnected mesh with node, element, region
+// and material numbers offset per mesh.
+
+namespace {
+
+enum { kLayNone = 0, kLayEl, kLayCn, kLayNd, kLayEl4 };
+enum { kOffNone = 0, kOffNode, kOffEl, kOffReg, kOffMat };
+struct FieldLayout {
+  int layout, off, is_int;
+};
+
+// How a dataAPI field concatenates: per element, per corner, per node or 4
+// per element, and the numbers its values hold.
+FieldLayout field_layout(int id) {
+  switch (id) {
+    case BL_ELDENSITY: case BL_ELENERGY: case BL_ELPRESSURE: case BL_ELCS2: case BL_ELVOLUME:
+    case BL_A1: case BL_A2: case BL_A3: case BL_B1: case BL_B2: case BL_B3: case BL_ELVISC:
+    case BL_ELMASS:
+      return {kLayEl, kOffNone, 0};
+    case BL_CNWT: case BL_CNX: case BL_CNY: case BL_CNVISCX: case BL_CNVISCY: case BL_CNMASS:
+    case BL_SPMASS:
+      return {kLayCn, kOffNone, 0};
+    case BL_NDX: case BL_NDY: case BL_NDU: case BL_NDV:
+      return {kLayNd, kOffNone, 0};
+    case BL_INDTYPE:
+      return {kLayNd, kOffReg, 1};  // interior nodes hold their region, boundary ones -bc
+    case BL_IELSORT1: case BL_IELSORT2:
+      return {kLayEl, kOffEl, 1};
+    case BL_IELND:
+      return {kLayEl4, kOffNode, 1};
+    case BL_IELEL:
+      return {kLayEl4, kOffEl, 1};
+    case BL_IELFC:
+      return {kLayEl4, kOffNone, 1};
+    case BL_IELMAT:
+      return {kLayEl, kOffMat, 1};
+    case BL_IELREG:
+      return {kLayEl, kOffReg, 1};
+    default:
+      return {kLayNone, kOffNone, 0};
+  }
+}
+
+size_t layout_count(int layout, const bl_sizes& s) {
+  return layout == kLayEl ? (size_t)s.nel
+                          : layout == kLayNd ? (size_t)s.nnd : 4 * (size_t)s.nel;
+}
+
+bool same_shared(const bl_config& a, const bl_config& b) {
+  return a.cvisc1 == b.cvisc1 && a.cvisc2 == b.cvisc2 && a.cfl_sf == b.cfl_sf &&
+         a.div_sf == b.div_sf && a.ztq == b.ztq && a.zhg == b.zhg && a.zsp == b.zsp &&
+         a.zcut == b.zcut && a.zerocut == b.zerocut && a.dencut == b.dencut &&
+         a.accut == b.accut && a.ccut == b.ccut && a.pcut == b.pcut &&
+         a.ale_zexist == b.ale_zexist && a.ale_zon == b.ale_zon && a.ale_zeul == b.ale_zeul &&
+         a.ale_adv_type == b.ale_adv_type && a.ale_mintime == b.ale_mintime &&
+         a.ale_maxtime == b.ale_maxtime && a.ale_sf == b.ale_sf;
+}
+
+// Copies mesh i's part of field id between the concatenated host array and
+// the mesh's own registered array (to_mesh: concatenated -> mesh).
+void batch_copy(bl_ctx* x, int id, bool to_mesh) {
+  const FieldLayout L = field_layout(id);
+  if (L.layout == kLayNone || L.is_int || !x->host[id]) return;
+  char* all = static_cast<char*>(x->host[id]);
+  for (int i = 0; i < x->ninst; i++) {
+    void* mine = x->inst_dh[i][id];
+    if (!mine) continue;
+    const size_t per = L.layout == kLayNd ? 1 : (L.layout == kLayEl ? 1 : 4);
+    const size_t b = (L.layout == kLayNd ? (size_t)x->nd_off[i] : (size_t)x->el_off[i]) * per;
+    const size_t n = (L.layout == kLayNd ? (size_t)(x->nd_off[i + 1] - x->nd_off[i])
+                                         : (size_t)(x->el_off[i + 1] - x->el_off[i])) * per;
+    if (to_mesh) std::memcpy(mine, all + 8 * b, 8 * n);
+    else std::memcpy(all + 8 * b, mine, 8 * n);
+  }
+}
+
+void fill_ts_batch(const bl_ctx* x, int i, const DevStep& S, bl_timestep* ts) {
+  ts->nstep = S.nstep;
+  ts->dt = S.dt;
+  ts->time = S.time;
+  ts->idtel = S.idtel;
+  std::memset(ts->sdt, 0, sizeof ts->sdt);
+  std::memcpy(ts->sdt, kSdt[S.sdt < 0 || S.sdt > 4 ? 0 : S.sdt], 8);
+  std::memset(ts->mdt, 0, sizeof ts->mdt);
+  const int nel_i = x->el_off[i + 1] - x->el_off[i];
+  if (S.idtel > 0 && S.idtel <= nel_i) {
+    int ii = x->ielmat_h[x->el_off[i] + S.idtel - 1];
+    if (ii > 0) {
+      ii -= x->mat_off[i];
+      ts->imdt = ii;
+      std::snprintf(ts->mdt, sizeof ts->mdt, "%10d", ii);
+    } else {
+      ts->imdt = 0;
+      std::memcpy(ts->mdt, "     MIXED", 10);
+    }
+  } else {
+    ts->imdt = -1;
+    std::memcpy(ts->mdt, "   UNKNOWN", 10);
+  }
+  ts->zcorrector = 1;
+  ts->dts = ts->dt;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bl_init_batch(bl_ctx** out, int ninst, const bl_sizes* sizes, const bl_config* configs,
+                  void* const* const* dh, int fp_mode, bl_error* error) {
+  set_err(error, BL_SUCCESS, BL_HALT_SINGLE, "");
+  if (!out || ninst < 1 || !sizes || !configs || !dh) {
+    set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init_batch: bad argument");
+    return BL_FAILURE;
+  }
+  *out = nullptr;
+  const bl_config& c0 = configs[0];
+  std::vector<int> el_off(ninst + 1, 0), nd_off(ninst + 1, 0), reg_off(ninst + 1, 0),
+      mat_off(ninst + 1, 0);
+  for (int i = 0; i < ninst; i++) {
+    const bl_sizes& s = sizes[i];
+    char msg[BL_SLEN + 1];
+    if (!dh[i] || s.nel < 1 || s.nnd < 4 || s.nreg < 1 || s.nreg > BL_MAXREG || s.nmat < 1 ||
+        s.nmat > BL_MAXMAT) {
+      std::snprintf(msg, sizeof msg, "ERROR: bl_init_batch: mesh %d: sizes out of range", i + 1);
+      set_err(error, BL_FAILURE, BL_HALT_ALL, msg);
+      return BL_FAILURE;
+    }
+    if (s.ncp != 0 || s.nmx != 0) {
+      std::snprintf(msg, sizeof msg, "ERROR: bl_init_batch: mesh %d has mixed cells", i + 1);
+      set_err(error, BL_FAILURE, BL_HALT_ALL, msg);
+      return BL_FAILURE;
+    }
+    if (!same_shared(configs[i], c0)) {
+      std::snprintf(msg, sizeof msg,
+                    "ERROR: bl_init_batch: mesh %d: hydro, cut-off or ALE settings differ", i + 1);
+      set_err(error, BL_FAILURE, BL_HALT_ALL, msg);
+      return BL_FAILURE;
+    }
+    if ((long long)el_off[i] + s.nel > 0x7fffffff || (long long)nd_off[i] + s.nnd > 0x7fffffff) {
+      set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init_batch: batch too large");
+      return BL_FAILURE;
+    }
+    el_off[i + 1] = el_off[i] + s.nel;
+    nd_off[i + 1] = nd_off[i] + s.nnd;
+    reg_off[i + 1] = reg_off[i] + s.nreg;
+    mat_off[i + 1] = mat_off[i] + s.nmat;
+  }
+  bl_sizes S{};
+  S.nel = S.nel1 = S.nel2 = el_off[ninst];
+  S.nnd = S.nnd1 = S.nnd2 = nd_off[ninst];
+  S.nsz = std::max(S.nel, S.nnd);
+  S.nreg = reg_off[ninst];
+  S.nmat = mat_off[ninst];
+  // the concatenated host arrays
+  std::vector<std::vector<char>> store(BL_NID + 1);
+  std::vector<void*> cdh(BL_NID + 1, nullptr);
+  for (int id = 1; id <= BL_NID; id++) {
+    const FieldLayout L = field_layout(id);
+    if (L.layout == kLayNone) continue;
+    int have = 0;
+    for (int i = 0; i < ninst; i++) have += dh[i][id] != nullptr;
+    if (have == 0) continue;
+    if (have != ninst) {
+      char msg[BL_SLEN + 1];
+      std::snprintf(msg, sizeof msg, "ERROR: bl_init_batch: field %d registered for some meshes only",
+                    id);
+      set_err(error, BL_FAILURE, BL_HALT_ALL, msg);
+      return BL_FAILURE;
+    }
+    const size_t esz = L.is_int ? 4 : 8;
+    store[id].resize(esz * layout_count(L.layout, S));
+    size_t at = 0;
+    for (int i = 0; i < ninst; i++) {
+      const size_t n = layout_count(L.layout, sizes[i]);
+      std::memcpy(store[id].data() + esz * at, dh[i][id], esz * n);
+      if (L.is_int && L.off != kOffNone) {
+        int* v = reinterpret_cast<int*>(store[id].data()) + at;
+        const int add = L.off == kOffNode ? nd_off[i] : L.off == kOffEl ? el_off[i]
+                      : L.off == kOffReg ? reg_off[i] : mat_off[i];
+        for (size_t k = 0; k < n; k++)
+          if (L.off == kOffNode || L.off == kOffEl || v[k] > 0) v[k] += add;
+      }
+      at += n;
+    }
+    cdh[id] = store[id].data();
+  }
+  // region and material tables: mesh after mesh; material 0 (void) once
+  Tables T;
+  T.et.push_back(c0.eos_type[0]);
+  for (int k = 0; k < BL_NEOSPARAM; k++) T.ep.push_back(c0.eos_param[0][k]);
+  for (int i = 0; i < ninst; i++) {
+    const bl_config& c = configs[i];
+    for (int r = 0; r < sizes[i].nreg; r++) {
+      T.kap.push_back(c.kappareg[r]);
+      T.pm.push_back(c.pmeritreg[r]);
+      T.zd.push_back(c.zdtnotreg[r]);
+      T.zm.push_back(c.zmidlength[r]);
+    }
+    for (int m = 1; m <= sizes[i].nmat; m++) {
+      T.et.push_back(c.eos_type[m]);
+      for (int k = 0; k < BL_NEOSPARAM; k++) T.ep.push_back(c.eos_param[m][k]);
+    }
+  }
+  bl_config C = c0;
+  int rc = init_impl(out, &S, &C, cdh.data(), fp_mode, error, &T);
+  if (rc != BL_SUCCESS) return rc;
+  bl_ctx* x = *out;
+  x->bstore = std::move(store);  // the context's host fields point into these
+  x->ninst = ninst;
+  x->el_off = el_off;
+  x->nd_off = nd_off;
+  x->mat_off = mat_off;
+  x->inst_dh.resize(ninst);
+  for (int i = 0; i < ninst; i++) x->inst_dh[i].assign(dh[i], dh[i] + BL_NID + 1);
+  // per-mesh controls and ownership tables
+  std::vector<bl::DevInst> inst(ninst);
+  std::vector<int> elinst(S.nel), ndinst(S.nnd), blkinst;
+  int nblk = 0;
+  for (int i = 0; i < ninst; i++) {
+    const bl_config& c = configs[i];
+    bl::DevInst& I = inst[i];
+    I.dt_g = c.dt_g;
+    I.dt_min = c.dt_min;
+    I.dt_max = c.dt_max;
+    I.dt_initial = c.dt_initial;
+    I.time_end = c.time_end;
+    I.el_begin = el_off[i];
+    I.el_end = el_off[i + 1];
+    I.blk_begin = nblk;
+    nblk += x->L.getdt_blocks(sizes[i].nel);
+    I.blk_end = nblk;
+    for (int k = el_off[i]; k < el_off[i + 1]; k++) elinst[k] = i;
+    for (int k = nd_off[i]; k < nd_off[i + 1]; k++) ndinst[k] = i;
+    blkinst.insert(blkinst.end(), I.blk_end - I.blk_begin, i);
+  }
+  cudaError_t st = cudaSuccess;
+  bl::DevFields& F = x->F;
+  F.steps = dalloc<DevStep>(x, ninst, st);
+  bl::DevInst* d_inst = dalloc<bl::DevInst>(x, ninst, st);
+  int* d_el = dalloc<int>(x, S.nel, st);
+  int* d_nd = dalloc<int>(x, S.nnd, st);
+  int* d_bk = dalloc<int>(x, nblk, st);
+  double* d_rv = dalloc<double>(x, 2L * nblk, st);
+  int* d_ri = dalloc<int>(x, 2L * nblk, st);
+  if (st != cudaSuccess || cudaMallocHost(&x->hsteps, sizeof(DevStep) * ninst) != cudaSuccess) {
+    bl_finalize(x);
+    *out = nullptr;
+    return cuda_fail(error, st == cudaSuccess ? cudaErrorMemoryAllocation : st, "bl_init_batch");
+  }
+  up(x, d_inst, inst.data(), ninst);
+  x->inst_h = inst;
+  up(x, d_el, elinst.data(), S.nel);
+  up(x, d_nd, ndinst.data(), S.nnd);
+  up(x, d_bk, blkinst.data(), nblk);
+  F.inst = d_inst;
+  F.elinst = d_el;
+  F.ndinst = d_nd;
+  F.blkinst = d_bk;
+  F.red_v = d_rv;  // partials of every mesh's blocks
+  F.red_i = d_ri;
+  F.ninst = ninst;
+  F.nblk_batch = nblk;
+  cudaError_t r = cudaStreamSynchronize(x->stream);
+  if (r != cudaSuccess) {
+    bl_finalize(x);
+    *out = nullptr;
+    return cuda_fail(error, r, "bl_init_batch");
+  }
+  return BL_SUCCESS;
+}
+
+int bl_run_batch(bl_ctx* x, bl_timestep* ts, int max_steps, int* status, int* nsteps,
+                 bl_error* e) {
+  set_err(e, BL_SUCCESS, BL_HALT_SINGLE, "");
+  if (nsteps) *nsteps = 0;
+  if (!x || !ts || max_steps < 0 || x->ninst < 1) {
+    set_err(e, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_run_batch: bad argument (or not a batch)");
+    return BL_FAILURE;
+  }
+  if (x->c.ale_zexist && x->c.ale_adv_type != 1) {
+    set_err(e, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_run_batch: only adv_type 1 runs on the device");
+    return BL_FAILURE;
+  }
+  const int n = x->ninst;
+  for (int i = 0; i < n; i++) {
+    DevStep& h = x->hsteps[i];
+    std::memset(&h, 0, sizeof h);
+    h.time = ts[i].time;
+    h.dt = ts[i].dt;
+    h.dts = ts[i].dts;
+    h.rdt = 1.0 / ts[i].dt;
+    h.nstep = ts[i].nstep;
+    h.idtel = ts[i].idtel;
+    h.run_mode = 1;
+    // a mesh already at its end time does not advance (the others do)
+    if (ts[i].time >= x->inst_h[i].time_end) h.stop_next = 1;
+  }
+  cudaMemcpyAsync(x->F.steps, x->hsteps, sizeof(DevStep) * n, cudaMemcpyHostToDevice, x->stream);
+  if (max_steps == 0) return bl_synchronize(x) == 0 ? BL_SUCCESS : BL_FAILURE;
+  const bool with_ale = x->c.ale_zexist != 0;
+  const int G = 16;  // steps per graph launch
+  cudaError_t r;
+  bl::DevFields F = x->F;
+  F.hist = nullptr;
+  bl::DevCfg C = x->C;
+  C.max_records = 0;
+  auto queue_step = [&]() {
+    x->L.getdt_b(F, C, x->stream);
+    x->L.lag_force_b(F, C, x->stream);
+    x->L.lag_accel_b(F, C, x->stream);
+    x->L.lag_state_b(F, C, x->stream);
+    if (with_ale) x->L.ale_b(F, C, x->stream);
+  };
+  if (!x->bexec || x->b_ale != with_ale) {
+    if (x->bexec) cudaGraphExecDestroy(x->bexec);
+    x->bexec = nullptr;
+    cudaGraph_t g;
+    r = cudaStreamBeginCapture(x->stream, cudaStreamCaptureModeThreadLocal);
+    if (r != cudaSuccess) return cuda_fail(e, r, "bl_run_batch capture");
+    for (int k = 0; k < G; k++) queue_step();
+    r = cudaStreamEndCapture(x->stream, &g);
+    if (r != cudaSuccess) return cuda_fail(e, r, "bl_run_batch capture");
+    r = cudaGraphInstantiate(&x->bexec, g, 0);
+    cudaGraphDestroy(g);
+    if (r != cudaSuccess) {
+      x->bexec = nullptr;
+      return cuda_fail(e, r, "bl_run_batch instantiate");
+    }
+    x->b_ale = with_ale;
+  }
+  const int per_step = bl::kLaunchesGetdt + bl::kLaunchesLagstep + (with_ale ? bl::kLaunchesAle : 0);
+  int done = 0;
+  while (done < max_steps) {
+    const int k = std::min(G, max_steps - done);
+    if (k == G) {
+      r = cudaGraphLaunch(x->bexec, x->stream);
+      if (r != cudaSuccess) return cuda_fail(e, r, "bl_run_batch launch");
+    } else {
+      for (int j = 0; j < k; j++) queue_step();
+    }
+    x->launches += (long long)k * per_step;
+    done += k;
+    cudaMemcpyAsync(x->hsteps, x->F.steps, sizeof(DevStep) * n, cudaMemcpyDeviceToHost, x->stream);
+    r = cudaStreamSynchronize(x->stream);
+    if (r != cudaSuccess) return cuda_fail(e, r, "bl_run_batch");
+    r = cudaGetLastError();
+    if (r != cudaSuccess) return cuda_fail(e, r, "bl_run_batch");
+    int active = 0;
+    for (int i = 0; i < n; i++) {
+      const DevStep& S = x->hsteps[i];
+      if (!(S.halted || S.stop_next || S.err_code || S.negvol_pred || S.negvol_corr ||
+            S.negvol_ale))
+        active++;
+    }
+    if (active == 0) break;
+  }
+  if (nsteps) *nsteps = done;
+  int first_bad = -1;
+  for (int i = 0; i < n; i++) {
+    const DevStep& S = x->hsteps[i];
+    fill_ts_batch(x, i, S, ts + i);
+    int code = 0;
+    if (S.err_code == 1 || S.err_code == 2) code = BL_FAILURE;
+    else if (S.negvol_pred) code = -S.negvol_pred;
+    else if (S.negvol_corr) code = -S.negvol_corr;
+    else if (S.negvol_ale) code = -S.negvol_ale;
+    if (status) status[i] = code;
+    if (code != 0 && first_bad < 0) first_bad = i;
+  }
+  x->cs2_is_v = false;
+  if (first_bad >= 0) {
+    const DevStep& S = x->hsteps[first_bad];
+    char msg[BL_SLEN + 1];
+    std::snprintf(msg, sizeof msg, "ERROR: mesh %d: %s", first_bad + 1,
+                  S.err_code == 1 ? "negative CFL condition in hydro_dr_getdt"
+                  : S.err_code == 2 ? "dt < dt_min"
+                                    : "negative volume in geometry_dr_getgeometry");
+    set_err(e, BL_FAILURE, S.err_code == 2 ? BL_HALT_ALL : BL_HALT_SINGLE, msg);
+    return BL_FAILURE;
+  }
+  return BL_SUCCESS;
+}
+
+int bl_batch_size(bl_ctx* x) { return x ? x->ninst : 0; }
 
 }  // extern "C"

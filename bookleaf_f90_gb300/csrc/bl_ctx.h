@@ -33,6 +33,15 @@ struct bl_ctx {
   cudaGraphExec_t call_exec[3] = {nullptr, nullptr, nullptr};
   bl::DevFields call_F[3] = {};
   bl::DevCfg call_C[3] = {};
+  // a batch of meshes (bl_init_batch); ninst = 0 for a single mesh
+  int ninst = 0;
+  std::vector<int> el_off, nd_off, mat_off;    // [ninst+1] first element, node, material
+  bl::DevStep* hsteps = nullptr;               // pinned mirror of F.steps
+  std::vector<bl::DevInst> inst_h;             // host copy of the per-mesh controls
+  std::vector<std::vector<void*>> inst_dh;     // each mesh's registered host arrays
+  std::vector<std::vector<char>> bstore;       // the concatenated host arrays, by field
+  cudaGraphExec_t bexec = nullptr;             // graph of batch steps
+  bool b_ale = false;
   // bl_run
   cudaGraphExec_t gexec = nullptr;
   int gsteps = 0;

@@ -47,6 +47,15 @@ struct DevStep {
   int pad;
 };
 
+// Per-mesh controls of a batch (independent meshes advanced together, each
+// with its own dt and time): the time-step parameters of its control file,
+// its element range and the k_getdt blocks that cover it.
+struct DevInst {
+  double dt_g, dt_min, dt_max, dt_initial, time_end;
+  int el_begin, el_end;
+  int blk_begin, blk_end;
+};
+
 struct StepRec {        // mirrors bl_step_record
   double time, dt;
   int nstep, idtel, sdt_code, ierr;
@@ -112,6 +121,13 @@ struct DevFields {
   int* red_i;                // [2*nblk]
   DevStep* step;
   StepRec* hist;
+  // batch (null in a single-mesh context)
+  DevStep* steps;            // [ninst] step headers
+  const DevInst* inst;       // [ninst]
+  const int* elinst;         // [nel] mesh of an element
+  const int* ndinst;         // [nnd] mesh of a node
+  const int* blkinst;        // [nblk_batch] mesh of a k_getdt block
+  int ninst, nblk_batch;
 };
 
 // ---------------------------------------------------------------- helpers

@@ -268,8 +268,8 @@ double* scratch(bl_ctx* x, size_t n) {
 
 extern "C" int bl_shortprint(bl_ctx* x, int table, double* out, int nflag, bl_error* e) {
   set_error(e, BL_SUCCESS, "");
-  if (!x || !out || (table != 0 && table != 1)) {
-    set_error(e, BL_FAILURE, "ERROR: bl_shortprint: bad argument");
+  if (!x || !out || (table != 0 && table != 1) || x->ninst > 0) {
+    set_error(e, BL_FAILURE, "ERROR: bl_shortprint: bad argument (or a batch context)");
     return BL_FAILURE;
   }
   const int nf = table == 1 ? x->s.nmat : x->s.nreg;
@@ -306,8 +306,8 @@ extern "C" int bl_shortprint(bl_ctx* x, int table, double* out, int nflag, bl_er
 extern "C" int bl_check_sod(bl_ctx* x, double time, double* l1_density, double* l1_energy,
                             bl_error* e) {
   set_error(e, BL_SUCCESS, "");
-  if (!x || !l1_density || !l1_energy) {
-    set_error(e, BL_FAILURE, "ERROR: bl_check_sod: bad argument");
+  if (!x || !l1_density || !l1_energy || x->ninst > 0) {
+    set_error(e, BL_FAILURE, "ERROR: bl_check_sod: bad argument (or a batch context)");
     return BL_FAILURE;
   }
   const int nb = blocks_for(x->s.nel);

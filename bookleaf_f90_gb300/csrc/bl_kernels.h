@@ -19,6 +19,11 @@ namespace bl {
   void launch_lag_accel(const DevFields& F, const DevCfg& C, cudaStream_t s);      \
   void launch_lag_state(const DevFields& F, const DevCfg& C, cudaStream_t s);      \
   void launch_ale(const DevFields& F, const DevCfg& C, cudaStream_t s);            \
+  void launch_getdt_batch(const DevFields& F, const DevCfg& C, cudaStream_t s);    \
+  void launch_lag_force_batch(const DevFields& F, const DevCfg& C, cudaStream_t s);\
+  void launch_lag_accel_batch(const DevFields& F, const DevCfg& C, cudaStream_t s);\
+  void launch_lag_state_batch(const DevFields& F, const DevCfg& C, cudaStream_t s);\
+  void launch_ale_batch(const DevFields& F, const DevCfg& C, cudaStream_t s);      \
   }
 
 BL_DECLARE_LAUNCHERS(fast)
@@ -31,6 +36,12 @@ struct Launchers {
   void (*lag_accel)(const DevFields&, const DevCfg&, cudaStream_t);
   void (*lag_state)(const DevFields&, const DevCfg&, cudaStream_t);
   void (*ale)(const DevFields&, const DevCfg&, cudaStream_t);
+  // the same over a batch of meshes (per-mesh step headers)
+  void (*getdt_b)(const DevFields&, const DevCfg&, cudaStream_t);
+  void (*lag_force_b)(const DevFields&, const DevCfg&, cudaStream_t);
+  void (*lag_accel_b)(const DevFields&, const DevCfg&, cudaStream_t);
+  void (*lag_state_b)(const DevFields&, const DevCfg&, cudaStream_t);
+  void (*ale_b)(const DevFields&, const DevCfg&, cudaStream_t);
 };
 
 // Kernels launched by one call of each launcher (for bl_kernel_launches).

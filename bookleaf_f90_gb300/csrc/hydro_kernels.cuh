@@ -488,6 +488,23 @@ __device__ __forceinline__ bool halted(const DevStep* S) {
   return *((volatile const int*)&S->halted) != 0;
 }
 
+// The step header of an element's or a node's mesh: the context's single
+// header, or in a batch the header of the mesh it belongs to; and the first
+// element of that mesh (element numbers reported to the host are local to
+// their mesh).
+template <bool BATCH>
+__device__ __forceinline__ DevStep* el_step(const DevFields& F, int iel) {
+  return BATCH ? F.steps + __ldg(F.elinst + iel) : F.step;
+}
+template <bool BATCH>
+__device__ __forceinline__ DevStep* nd_step(const DevFields& F, int ind) {
+  return BATCH ? F.steps + __ldg(F.ndinst + ind) : F.step;
+}
+template <bool BATCH>
+__device__ __forceinline__ int el_base(const DevFields& F, int iel) {
+  return BATCH ? F.inst[__ldg(F.elinst + iel)].el_begin : 0;
+}
+
 // ================================================================ k_getdt
 
 // (value,index) pairs for the two scans.  CFL: smallest value, first index
@@ -551,9 +568,13 @@ __device__ __forceinline__ void getdt_tail(const DevFields& F, const DevCfg& C, 
 
 // The block reduction of the candidates, the last block's reduction of the
 // block partials and time_dr_end (time_dr_advance.f90:74-132)
-template <int BS>
+// over the k_getdt blocks [blk0, blk0 + nblk) of one mesh (all of them for
+// a single mesh; a batch's mesh in a batch, whose time-step parameters then
+// come from I, and whose element numbers start at el0)
+template <int BS, bool BATCH>
 __device__ __forceinline__ void getdt_finish(const DevFields& F, const DevCfg& C, DevStep* S,
-                                             double cflv, int cfli, double divv, int divi) {
+                                             double cflv, int cfli, double divv, int divi,
+                                             int blk0, int nblk, int el0, const DevInst* I) {
   // ---- block reduction
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -586,7 +607,7 @@ __device__ __forceinline__ void getdt_finish(const DevFields& F, const DevCfg& C
     F.red_i[2 * blockIdx.x + 1] = divi;
     __threadfence();
     unsigned int t = atomicAdd(&S->ticket, 1u);
-    s_last = (t == gridDim.x - 1);
+    s_last = (t == (unsigned int)(nblk - 1));
   }
   __syncthreads();
   if (!s_last) return;
@@ -601,9 +622,9 @@ __device__ __forceinline__ void getdt_finish(const DevFields& F, const DevCfg& C
   // other blocks' writes) are all in flight before the first comparison.
   {
     constexpr int U = 8;
-    const double2* rv = reinterpret_cast<const double2*>(F.red_v);
-    const int2* ri = reinterpret_cast<const int2*>(F.red_i);
-    const int nb = (int)gridDim.x;
+    const double2* rv = reinterpret_cast<const double2*>(F.red_v) + blk0;
+    const int2* ri = reinterpret_cast<const int2*>(F.red_i) + blk0;
+    const int nb = nblk;
     for (int b0 = threadIdx.x; b0 < nb; b0 += BS * U) {
       double2 v[U];
       int2 ix[U];
@@ -657,31 +678,37 @@ __device__ __forceinline__ void getdt_finish(const DevFields& F, const DevCfg& C
   }
   const double rdt_cfl = C.cfl_sf * SQRT(cflv);
   const double rdt_div = DIV(C.div_sf, divv);
+  // 1-based element numbers local to the mesh (0: none)
+  const int cfln = cfli >= 0 && cfli != 0x7fffffff ? cfli - el0 + 1 : 0;
+  const int divn = divi >= 0 ? divi - el0 + 1 : 0;
+  const double dt_max = BATCH ? I->dt_max : C.dt_max, dt_g = BATCH ? I->dt_g : C.dt_g;
+  const double dt_initial = BATCH ? I->dt_initial : C.dt_initial;
+  const double dt_min = BATCH ? I->dt_min : C.dt_min, time_end = BATCH ? I->time_end : C.time_end;
   S->cfl_rdt = rdt_cfl;
-  S->cfl_idt = cfli + 1;
+  S->cfl_idt = cfln;
   S->div_rdt = rdt_div;
-  S->div_idt = divi + 1;
-  double mind = C.dt_max;
+  S->div_idt = divn;
+  double mind = dt_max;
   int mini = -1, mins = 0;
-  double g = C.dt_g * S->dt;
+  double g = dt_g * S->dt;
   if (g < mind) { mind = g; mini = -1; mins = 1; }
-  if (S->nstep == 0 && C.dt_initial < mind) { mind = C.dt_initial; mini = -1; mins = 2; }
-  if (rdt_cfl < mind) { mind = rdt_cfl; mini = cfli + 1; mins = 3; }
-  if (rdt_div < mind) { mind = rdt_div; mini = divi + 1; mins = 4; }
+  if (S->nstep == 0 && dt_initial < mind) { mind = dt_initial; mini = -1; mins = 2; }
+  if (rdt_cfl < mind) { mind = rdt_cfl; mini = cfln; mins = 3; }
+  if (rdt_div < mind) { mind = rdt_div; mini = divn; mins = 4; }
   S->nstep = S->nstep + 1;
   S->dt = mind;
   S->rdt = DIV(1.0, mind);
   S->sdt = mins;
   S->idtel = mini;
   S->time = S->time + mind;
-  if (mind < C.dt_min) {
+  if (mind < dt_min) {
     S->ierr = -1;
     S->iout = 1;
     S->err_code = 2;
     if (S->run_mode) S->halted = 1;
   }
   if (S->run_mode) {
-    if (S->time >= C.time_end) S->stop_next = 1;
+    if (S->time >= time_end) S->stop_next = 1;
     int r = S->nrecord;
     if (F.hist && r < C.max_records) {
       F.hist[r].time = S->time;
@@ -746,17 +773,30 @@ __device__ __forceinline__ double nb_ratio(const FaceQ& f, double ddx, double dd
 // generated meshes elements are numbered along mesh lines, so the face
 // across face 2 and the two limiter neighbours of side 0 are the adjacent
 // elements and take the shared path.
-template <int BS>
+template <int BS, bool BATCH>
 __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg C) {
+  // the mesh of this block: the context's, or in a batch the block's own
+  // (its blocks [blk0, blk0 + nblk), elements [el0, el1))
   DevStep* S = F.step;
+  int blk0 = 0, nblk = (int)gridDim.x, el0 = 0, el1 = F.nel;
+  const DevInst* I = nullptr;
+  if (BATCH) {
+    const int m = __ldg(F.blkinst + blockIdx.x);
+    I = F.inst + m;
+    S = F.steps + m;
+    blk0 = I->blk_begin;
+    nblk = I->blk_end - I->blk_begin;
+    el0 = I->el_begin;
+    el1 = I->el_end;
+  }
   if (halted(S)) return;
   if (S->stop_next) {            // bl_run: the previous step reached time_end
-    if (blockIdx.x == 0 && threadIdx.x == 0) S->halted = 1;
+    if ((int)blockIdx.x == blk0 && threadIdx.x == 0) S->halted = 1;
     return;
   }
   const int t = threadIdx.x;
-  const int iel = blockIdx.x * (BS - 2) + t - 1;
-  const bool inmesh = iel >= 0 && iel < F.nel;
+  const int iel = el0 + ((int)blockIdx.x - blk0) * (BS - 2) + t - 1;
+  const bool inmesh = iel >= el0 && iel < el1;
   const bool own = inmesh && t > 0 && t < BS - 1;
   double cflv = HUGE_VAL;        // sentinel above HUGE(1.0)
   int cfli = 0x7fffffff;
@@ -957,27 +997,40 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
     }
     getdt_tail(F, C, iel, x, y, u, v, visc, cflv, cfli, divv, divi);
   }
-  getdt_finish<BS>(F, C, S, cflv, cfli, divv, divi);
+  getdt_finish<BS, BATCH>(F, C, S, cflv, cfli, divv, divi, blk0, nblk, el0, I);
 }
 
 template <int BS>
 constexpr int getdt_elements_per_block() { return BS - 2; }
 #else
 
-template <int BS>
+template <int BS, bool BATCH>
 __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg C) {
+  // the mesh of this block: the context's, or in a batch the block's own
+  // (its blocks [blk0, blk0 + nblk), elements [el0, el1))
   DevStep* S = F.step;
+  int blk0 = 0, nblk = (int)gridDim.x, el0 = 0, el1 = F.nel;
+  const DevInst* I = nullptr;
+  if (BATCH) {
+    const int m = __ldg(F.blkinst + blockIdx.x);
+    I = F.inst + m;
+    S = F.steps + m;
+    blk0 = I->blk_begin;
+    nblk = I->blk_end - I->blk_begin;
+    el0 = I->el_begin;
+    el1 = I->el_end;
+  }
   if (halted(S)) return;
   if (S->stop_next) {            // bl_run: the previous step reached time_end
-    if (blockIdx.x == 0 && threadIdx.x == 0) S->halted = 1;
+    if ((int)blockIdx.x == blk0 && threadIdx.x == 0) S->halted = 1;
     return;
   }
-  const int iel = blockIdx.x * BS + threadIdx.x;
+  const int iel = el0 + ((int)blockIdx.x - blk0) * BS + threadIdx.x;
   double cflv = HUGE_VAL;        // sentinel above HUGE(1.0)
   int cfli = 0x7fffffff;
   double divv = DBL_MIN;         // TINY(1.0)
   int divi = -1;
-  if (iel < F.nel) {
+  if (iel < el1) {
     const int4 nd = __ldg(F.ielnd + iel);
     const int n[4] = {nd.x, nd.y, nd.z, nd.w};
     double x[4], y[4], u[4], v[4];
@@ -1119,7 +1172,7 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
     }
     getdt_tail(F, C, iel, x, y, u, v, visc, cflv, cfli, divv, divi);
   }
-  getdt_finish<BS>(F, C, S, cflv, cfli, divv, divi);
+  getdt_finish<BS, BATCH>(F, C, S, cflv, cfli, divv, divi, blk0, nblk, el0, I);
 }
 
 template <int BS>
@@ -1128,12 +1181,12 @@ constexpr int getdt_elements_per_block() { return BS; }
 
 // ================================================================ k_lag_force
 
-template <int BS>
+template <int BS, bool BATCH>
 __global__ void __launch_bounds__(BS, BL_FORCE_MINB) k_lag_force(DevFields F, DevCfg C) {
-  const DevStep* S = F.step;
-  if (halted(S)) return;
   const int iel = blockIdx.x * BS + threadIdx.x;
   if (iel >= F.nel) return;
+  DevStep* S = el_step<BATCH>(F, iel);
+  if (halted(S)) return;
   const double dt = S->dt;
   const double hdt = 0.5 * dt;   // time_dr_setpredictor dts / getvertex step
   const double zc = C.zerocut;
@@ -1177,7 +1230,7 @@ __global__ void __launch_bounds__(BS, BL_FORCE_MINB) k_lag_force(DevFields F, De
   }
   // ---- geometry, density (geometry_dr_getgeometry, density_dr_getdensity)
   Iso g = getiso(xh, yh);
-  if (gtF(0.0, g.vol)) atomicMax(&F.step->negvol_pred, iel + 1);
+  if (gtF(0.0, g.vol)) atomicMax(&S->negvol_pred, iel + 1 - el_base<BATCH>(F, iel));
   const double rho = DIV(m, g.vol);
   // ---- energy (hydro_kn_getenergy with dts = dt/2) and EoS
   const double eh = energy_update(e0, m, zc, hdt, fx, fy, u, v);
@@ -1245,12 +1298,12 @@ __global__ void __launch_bounds__(BS, BL_FORCE_MINB) k_lag_force(DevFields F, De
 
 // ================================================================ k_lag_accel
 
-template <int BS>
+template <int BS, bool BATCH>
 __global__ void BL_ACCEL_BOUNDS(BS) k_lag_accel(DevFields F, DevCfg C) {
-  const DevStep* S = F.step;
-  if (halted(S)) return;
   const int ind = blockIdx.x * BS + threadIdx.x;
   if (ind >= F.nnd) return;
+  const DevStep* S = nd_step<BATCH>(F, ind);
+  if (halted(S)) return;
   const double dt = S->dt;
   const double zc = C.zerocut;
   // hydro_kn_scatteracceleration: corner-major order over ielsort
@@ -1313,12 +1366,12 @@ __global__ void BL_ACCEL_BOUNDS(BS) k_lag_accel(DevFields F, DevCfg C) {
 
 // ================================================================ k_lag_state
 
-template <int BS>
+template <int BS, bool BATCH>
 __global__ void BL_STATE_BOUNDS(BS) k_lag_state(DevFields F, DevCfg C) {
-  const DevStep* S = F.step;
-  if (halted(S)) return;
   const int iel = blockIdx.x * BS + threadIdx.x;
   if (iel >= F.nel) return;
+  DevStep* S = el_step<BATCH>(F, iel);
+  if (halted(S)) return;
   const double dt = S->dt;
   const double zc = C.zerocut;
   const int4 nd = __ldg(F.ielnd + iel);
@@ -1332,7 +1385,7 @@ __global__ void BL_STATE_BOUNDS(BS) k_lag_state(DevFields F, DevCfg C) {
     vb[j] = F.ndvbar[n[j]];
   }
   Iso g = getiso(x, y);
-  if (gtF(0.0, g.vol)) atomicMax(&F.step->negvol_corr, iel + 1);
+  if (gtF(0.0, g.vol)) atomicMax(&S->negvol_corr, iel + 1 - el_base<BATCH>(F, iel));
   const double m = F.mass[iel];
   const double rho = DIV(m, g.vol);
   const d4 f4x = F.cnfx[iel], f4y = F.cnfy[iel];
@@ -1394,16 +1447,30 @@ int getdt_blocks(int nel) {
 }
 
 void launch_getdt(const DevFields& F, const DevCfg& C, cudaStream_t s) {
-  k_getdt<BS_DT><<<getdt_blocks(F.nel), BS_DT, 0, s>>>(F, C);
+  k_getdt<BS_DT, false><<<getdt_blocks(F.nel), BS_DT, 0, s>>>(F, C);
 }
 void launch_lag_force(const DevFields& F, const DevCfg& C, cudaStream_t s) {
-  k_lag_force<BS_EL><<<(F.nel + BS_EL - 1) / BS_EL, BS_EL, 0, s>>>(F, C);
+  k_lag_force<BS_EL, false><<<(F.nel + BS_EL - 1) / BS_EL, BS_EL, 0, s>>>(F, C);
 }
 void launch_lag_accel(const DevFields& F, const DevCfg& C, cudaStream_t s) {
-  k_lag_accel<BS_ND><<<(F.nnd + BS_ND - 1) / BS_ND, BS_ND, 0, s>>>(F, C);
+  k_lag_accel<BS_ND, false><<<(F.nnd + BS_ND - 1) / BS_ND, BS_ND, 0, s>>>(F, C);
 }
 void launch_lag_state(const DevFields& F, const DevCfg& C, cudaStream_t s) {
-  k_lag_state<BS_EL><<<(F.nel + BS_EL - 1) / BS_EL, BS_EL, 0, s>>>(F, C);
+  k_lag_state<BS_EL, false><<<(F.nel + BS_EL - 1) / BS_EL, BS_EL, 0, s>>>(F, C);
+}
+// a batch of meshes: k_getdt over each mesh's own blocks, the rest over all
+// elements or nodes, each reading the step header of its mesh
+void launch_getdt_batch(const DevFields& F, const DevCfg& C, cudaStream_t s) {
+  k_getdt<BS_DT, true><<<F.nblk_batch, BS_DT, 0, s>>>(F, C);
+}
+void launch_lag_force_batch(const DevFields& F, const DevCfg& C, cudaStream_t s) {
+  k_lag_force<BS_EL, true><<<(F.nel + BS_EL - 1) / BS_EL, BS_EL, 0, s>>>(F, C);
+}
+void launch_lag_accel_batch(const DevFields& F, const DevCfg& C, cudaStream_t s) {
+  k_lag_accel<BS_ND, true><<<(F.nnd + BS_ND - 1) / BS_ND, BS_ND, 0, s>>>(F, C);
+}
+void launch_lag_state_batch(const DevFields& F, const DevCfg& C, cudaStream_t s) {
+  k_lag_state<BS_EL, true><<<(F.nel + BS_EL - 1) / BS_EL, BS_EL, 0, s>>>(F, C);
 }
 
 }  // namespace BL_NS

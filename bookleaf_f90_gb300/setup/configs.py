@@ -33,11 +33,19 @@ def _mesh(nx, ny, x0, y0, x1, y1, bcs):
 """
 
 
-def sod(nx=400, ny=40, time_end=0.2, eulerian=False, scale=1.0):
+def sod(nx=400, ny=40, time_end=0.2, eulerian=False, scale=1.0, gamma=1.4, pratio=10.0):
+    """Sod shock tube.  ``gamma`` and the pressure ratio ``pratio`` of the
+    left (rho 1, p 1) and right (rho 0.125, p 1/pratio) states default to the
+    classic problem (e = 2.5 and 2.0)."""
     L = 1.0 * scale
     H = 0.1 * scale
     ale = "&ALE\n zeul=.TRUE.\n/\n" if eulerian else ""
     s = scale
+    if gamma == 1.4 and pratio == 10.0:
+        e_left, e_right = 2.5, 2.0
+    else:
+        e_left = 1.0 / ((gamma - 1.0) * 1.0)
+        e_right = (1.0 / pratio) / ((gamma - 1.0) * 0.125)
     return f"""&CONTROL
  time_start=0.0
  time_end={time_end!r}
@@ -51,7 +59,7 @@ def sod(nx=400, ny=40, time_end=0.2, eulerian=False, scale=1.0):
 /
 &EOS
  eos_type(1)='ideal gas'
- eos_param(1,1)=1.4
+ eos_param(1,1)={gamma!r}
 /
 """ + _mesh(nx, ny, 0.0, 0.0, L, H, ("SLIPY", "SLIPX", "SLIPY", "SLIPX")) + ale + f"""&INDICATORS
  region_type(1)='background'
@@ -66,11 +74,11 @@ def sod(nx=400, ny=40, time_end=0.2, eulerian=False, scale=1.0):
  thermodynamic_type(1)='region'
  thermodynamic_value(1)=1
  density(1)=1.0
- energy(1)=2.5
+ energy(1)={e_left!r}
  thermodynamic_type(2)='region'
  thermodynamic_value(2)=2
  density(2)=0.125
- energy(2)=2.0
+ energy(2)={e_right!r}
 /
 &SHAPES
  shape_type(1)='rectangle'

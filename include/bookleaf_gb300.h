@@ -196,6 +196,35 @@ int bl_sync_to_host(bl_ctx *ctx, int id);
 /* Uploads host field id again after the host changed it (id = 0: all). */
 int bl_sync_to_device(bl_ctx *ctx, int id);
 
+/* ---- batches of meshes (no counterpart in the reference) ------------------
+ * Several independent problems -- each what one control file describes, with
+ * its own mesh, materials, time-step controls and end time -- advanced
+ * together: one kernel per phase over all of them, each mesh keeping its own
+ * dt and time on the device.  The results of every mesh are those of running
+ * it alone (bit for bit in BL_FP_EXACT).
+ *
+ * bl_init_batch: ninst meshes; sizes[i], configs[i] and the dataAPI table
+ * dh[i] describe mesh i exactly as bl_init's arguments do (the same fields
+ * registered for every mesh).  The hydro, cut-off and ALE settings must be
+ * the same for all meshes; the time-step controls, regions and materials
+ * may differ.  Mixed cells are not supported in a batch.  The solver entry
+ * points, bl_run, bl_time_step_kernels and the diagnostics refuse a batch
+ * context; bl_sync_to_host / bl_sync_to_device move every mesh's own arrays.
+ *
+ * bl_run_batch: advances all meshes on the device (graphs of 16 steps) from
+ * ts[0..ninst-1] until each has reached its time_end or stopped on an error,
+ * or max_steps steps have run (a mesh already at its time_end does not
+ * advance); ts[i] receives mesh i's timestep, status[i]
+ * (may be NULL) its error%ierr (0, -1, or -iel of a negative volume), and
+ * *nsteps the number of steps run.  Returns BL_SUCCESS when no mesh failed,
+ * else BL_FAILURE with err naming the first failed mesh. */
+int bl_init_batch(bl_ctx **ctx, int ninst, const bl_sizes *sizes, const bl_config *configs,
+                  void *const *const *dh, int fp_mode, bl_error *err);
+int bl_run_batch(bl_ctx *ctx, bl_timestep *ts, int max_steps, int *status, int *nsteps,
+                 bl_error *err);
+/* Number of meshes of a batch context (0 for a single mesh). */
+int bl_batch_size(bl_ctx *ctx);
+
 /* ---- introspection ------------------------------------------------------- */
 
 /* Waits for the context's stream.  Returns 0 or a CUDA error number. */

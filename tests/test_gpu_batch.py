@@ -1,0 +1,107 @@
+"""A batch of independent problems (bl_init_batch / bl_run_batch) advances
+every mesh as it would alone: each mesh's final fields and timestep equal
+those of running it by itself with the device loop, bit for bit, in exact
+and in fast mode.  The meshes differ in size, gamma, pressure ratio,
+time-step controls and end time, so they take different dt sequences and
+finish at different steps."""
+import ctypes as ct
+
+import pytest
+
+from bookleaf_f90_gb300 import BatchSolver, Problem, Solver, SolverError, abi, configs
+from helpers import compare
+
+pytestmark = pytest.mark.gpu
+
+LAGRANGIAN = [
+    configs.sod(24, 4, time_end=0.05),
+    configs.sedov(16, time_end=0.02),
+    configs.sod(30, 3, time_end=0.03, gamma=1.6, pratio=100.0),
+    configs.sedov(12, time_end=0.05, gamma=1.25),
+]
+EULERIAN = [
+    configs.sod(20, 4, time_end=0.03, eulerian=True),
+    configs.sedov(14, time_end=0.02, eulerian=True, gamma=1.6),
+    configs.sod(16, 2, time_end=0.02, eulerian=True, gamma=1.3, pratio=1000.0),
+]
+
+
+def _alone(deck, fp):
+    p = Problem.from_deck(deck)
+    s = Solver(p, fp_mode=fp)
+    ierr, _ = s.run(history=False)
+    s.sync_to_host(0)
+    s.close()
+    return ierr, p
+
+
+def _same_timestep(a, b):
+    return ((a.nstep, a.time, a.dt, a.idtel, bytes(a.sdt), a.imdt) ==
+            (b.nstep, b.time, b.dt, b.idtel, bytes(b.sdt), b.imdt))
+
+
+@pytest.mark.parametrize("fp", [abi.FP_EXACT, abi.FP_FAST], ids=["exact", "fast"])
+@pytest.mark.parametrize("decks", [LAGRANGIAN, EULERIAN], ids=["lagrangian", "eulerian"])
+def test_batch_equals_each_mesh_alone(decks, fp):
+    probs = [Problem.from_deck(d) for d in decks]
+    b = BatchSolver(probs, fp_mode=fp)
+    ierr, status, nsteps = b.run()
+    assert ierr == 0 and status == [0] * len(decks), b.error.message
+    b.sync_to_host(0)
+    steps = []
+    for d, p in zip(decks, probs):
+        ierr1, q = _alone(d, fp)
+        assert ierr1 == 0
+        assert _same_timestep(p.timestep, q.timestep), (p.timestep.as_tuple(), q.timestep.as_tuple())
+        assert not compare(p, q, exact=True)
+        steps.append(p.timestep.nstep)
+    assert len(set(steps)) > 1          # the meshes really ran different step counts
+    assert max(steps) <= nsteps < max(steps) + 16
+    b.close()
+
+
+def test_batch_step_limit_then_resume():
+    """A run stopped after k steps and resumed ends where one run ends."""
+    probs = [Problem.from_deck(d) for d in LAGRANGIAN]
+    b = BatchSolver(probs, fp_mode=abi.FP_EXACT)
+    ierr, status, n1 = b.run(max_steps=21)
+    assert ierr == 0 and n1 == 21
+    assert all(p.timestep.nstep <= 21 for p in probs)
+    ierr, status, n2 = b.run()
+    assert ierr == 0, b.error.message
+    b.sync_to_host(0)
+    for d, p in zip(LAGRANGIAN, probs):
+        _, q = _alone(d, abi.FP_EXACT)
+        assert _same_timestep(p.timestep, q.timestep)
+        assert not compare(p, q, exact=True)
+
+
+def test_failing_mesh_reports_its_status_and_leaves_the_others():
+    """A mesh that stops on dt < dt_min reports it in its own status; the
+    other meshes of the batch run on to their end times unchanged."""
+    bad = configs.sod(16, 4, time_end=0.05).replace("dt_min=1e-10", "dt_min=0.5").replace(
+        "dt_max=0.001", "dt_max=1.0")
+    decks = [LAGRANGIAN[0], bad, LAGRANGIAN[1]]
+    probs = [Problem.from_deck(d) for d in decks]
+    b = BatchSolver(probs, fp_mode=abi.FP_EXACT)
+    ierr, status, _ = b.run()
+    assert ierr != 0 and status == [0, abi.FAILURE, 0]
+    assert "mesh 2" in b.error.message and "dt < dt_min" in b.error.message
+    b.sync_to_host(0)
+    for i in (0, 2):
+        _, q = _alone(decks[i], abi.FP_EXACT)
+        assert _same_timestep(probs[i].timestep, q.timestep)
+        assert not compare(probs[i], q, exact=True)
+
+
+def test_batch_rejects_different_settings_and_single_mesh_calls():
+    with pytest.raises(SolverError, match="settings differ"):
+        BatchSolver([Problem.from_deck(LAGRANGIAN[0]), Problem.from_deck(EULERIAN[0])])
+    probs = [Problem.from_deck(d) for d in LAGRANGIAN[:2]]
+    b = BatchSolver(probs, fp_mode=abi.FP_EXACT)
+    assert b.L.bl_batch_size(b.ctx) == 2
+    err = abi.Error()
+    ts = probs[0].timestep
+    assert b.L.bl_getdt(b.ctx, ct.byref(ts), ct.byref(err)) == abi.FAILURE
+    assert "batch context" in err.message
+    b.close()
