@@ -229,3 +229,31 @@ def sod_multimaterial(nx=100, ny=25, time_end=20.0, vf=0.5):
  shape_param(1,:)=50.5,-10.0,150.0,50.0,{vf!r}
 /
 """
+
+
+def ensemble(n=512, seed=20240607, side_min=32, side_max=512):
+    """Decks of a seeded ensemble of independent Eulerian problems: half Sod
+    (gamma ~ U(1.2, 1.8), pressure ratio ~ logU(2, 1e4), density ratio 8,
+    t = 0.2) and half Sedov (gamma ~ U(1.2, 1.8), t = 1.0), mesh side ~
+    logU(side_min, side_max); a Sod tube of side s has about s^2 square
+    cells (s*sqrt(10) x s/sqrt(10)).  Returns [(deck, meta)] with meta the
+    drawn parameters."""
+    import math
+    import random
+    rng = random.Random(seed)
+    out = []
+    for i in range(n):
+        side = int(round(math.exp(rng.uniform(math.log(side_min), math.log(side_max)))))
+        gamma = rng.uniform(1.2, 1.8)
+        if i % 2 == 0:
+            ratio = math.exp(rng.uniform(math.log(2.0), math.log(1.0e4)))
+            nx = max(4, int(round(side * math.sqrt(10.0))))
+            ny = max(2, int(round(side / math.sqrt(10.0))))
+            deck = sod(nx, ny, time_end=0.2, eulerian=True, gamma=gamma, pratio=ratio)
+            meta = {"kind": "sod", "side": side, "nx": nx, "ny": ny, "gamma": gamma,
+                    "pratio": ratio}
+        else:
+            deck = sedov(side, time_end=1.0, eulerian=True, gamma=gamma)
+            meta = {"kind": "sedov", "side": side, "nx": side, "ny": side, "gamma": gamma}
+        out.append((deck, meta))
+    return out
