@@ -193,8 +193,9 @@ def run_ensemble(args, torch):
             np.copyto(p.fields[fid], a)
         ct.memmove(ct.addressof(p.timestep), ct.addressof(init[i][1]), ct.sizeof(abi.Timestep))
 
-    # ---- batched
+    # ---- batched: autotune (steps per graph, node block size), warm up
     b = BatchSolver(probs, fp_mode=fp)
+    tg, tb, tms = b.autotune()
     ierr, _, _ = b.run(max_steps=W)
     assert ierr == 0, b.error.message
     for i, p in enumerate(probs):
@@ -265,7 +266,9 @@ def run_ensemble(args, torch):
                        "nel_max": max(nels), "fp_mode": args.fp,
                        "meshes_active_whole_window": active,
                        "timed": "%d steps from t=0" % nsteps,
-                       "loop": "bl_run_batch, CUDA graphs of 16 steps",
+                       "loop": "bl_run_batch, CUDA graphs of %d steps" % tg,
+                       "autotune": {"graph_steps": tg, "node_block": tb,
+                                    "ms_per_step": {"%d,%d" % k: v for k, v in tms.items()}},
                        "setup_s": setup_s},
             "plain_per_mesh": {"value": plain, "unit": "zone-cycles/s", "ms_total": ms_p,
                                "how": "each mesh alone through bl_run, the same %d steps "

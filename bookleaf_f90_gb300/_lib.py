@@ -61,6 +61,9 @@ def load(build_if_missing=True):
     L.bl_run_batch.restype = ct.c_int
     L.bl_batch_size.argtypes = [vp]
     L.bl_batch_size.restype = ct.c_int
+    L.bl_autotune_batch.argtypes = [vp, vp, P(ct.c_int), P(ct.c_int), P(ct.c_double), ct.c_int,
+                                    P(abi.Error)]
+    L.bl_autotune_batch.restype = ct.c_int
     L.bl_fp64_rates.restype = ct.c_int
     L.bl_shortprint.argtypes = [vp, ct.c_int, P(ct.c_double), ct.c_int, P(abi.Error)]
     L.bl_shortprint.restype = ct.c_int
@@ -77,7 +80,7 @@ EXPORTS = ("bl_init", "bl_finalize", "bl_getdt", "bl_lagstep", "bl_alestep", "bl
            "bl_sync_to_host", "bl_sync_to_device", "bl_synchronize", "bl_stream",
            "bl_kernel_launches", "bl_version", "bl_getdt_noalloc", "bl_selftest_fp64",
            "bl_fp64_rates", "bl_shortprint", "bl_check_sod", "bl_time_step_kernels",
-           "bl_init_batch", "bl_run_batch", "bl_batch_size")
+           "bl_init_batch", "bl_run_batch", "bl_batch_size", "bl_autotune_batch")
 
 
 def fp64_rates():

@@ -50,6 +50,22 @@ class BatchSolver:
             ct.memmove(ct.addressof(p.timestep), ct.addressof(t), ct.sizeof(abi.Timestep))
         return ierr, list(status), nsteps.value
 
+    def autotune(self):
+        """Chooses the steps per graph and the node kernels' block size by
+        timing each candidate from the Problems' current arrays (which it
+        uploads again afterwards).  Returns (steps per graph, block size,
+        {(steps, block): ms per step})."""
+        n = len(self.problems)
+        ts = (abi.Timestep * n)(*[p.timestep for p in self.problems])
+        g, bs = ct.c_int(0), ct.c_int(0)
+        ms = (ct.c_double * 9)()
+        ierr = self.L.bl_autotune_batch(self.ctx, ct.cast(ts, ct.c_void_p), ct.byref(g),
+                                        ct.byref(bs), ms, 9, ct.byref(self.error))
+        if ierr != 0:
+            raise SolverError(ierr, self.error.iout, self.error.message)
+        cand = [(G, B) for G in (8, 16, 32) for B in (128, 256, 512)]
+        return g.value, bs.value, dict(zip(cand, list(ms)))
+
     def sync_to_host(self, fid=0):
         return self.L.bl_sync_to_host(self.ctx, fid)
 

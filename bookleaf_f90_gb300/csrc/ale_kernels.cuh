@@ -487,7 +487,14 @@ void launch_ale_t(const DevFields& F, const DevCfg& C, cudaStream_t s) {
   const int ge = (F.nel + BS_A - 1) / BS_A;
   k_ale_flux<BS_A, BATCH><<<ge, BS_A, 0, s>>>(F, C);
   k_ale_el<BS_A, BATCH><<<ge, BS_A, 0, s>>>(F, C);
-  k_ale_nd<BS_AN, BATCH><<<(F.nnd + BS_AN - 1) / BS_AN, BS_AN, 0, s>>>(F, C);
+  if constexpr (!BATCH) {
+    k_ale_nd<BS_AN, false><<<(F.nnd + BS_AN - 1) / BS_AN, BS_AN, 0, s>>>(F, C);
+  } else {
+    // block size chosen by the batch's autotuner (128, 256 or 512)
+    if (F.nd_block == 128) k_ale_nd<128, true><<<(F.nnd + 127) / 128, 128, 0, s>>>(F, C);
+    else if (F.nd_block == 512) k_ale_nd<512, true><<<(F.nnd + 511) / 512, 512, 0, s>>>(F, C);
+    else k_ale_nd<256, true><<<(F.nnd + 255) / 256, 256, 0, s>>>(F, C);
+  }
   k_ale_update<BS_A, BATCH><<<ge, BS_A, 0, s>>>(F, C);
 }
 void launch_ale(const DevFields& F, const DevCfg& C, cudaStream_t s) {

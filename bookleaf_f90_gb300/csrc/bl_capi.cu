@@ -1353,6 +1353,7 @@ int bl_init_batch(bl_ctx** out, int ninst, const bl_sizes* sizes, const bl_confi
   F.red_i = d_ri;
   F.ninst = ninst;
   F.nblk_batch = nblk;
+  F.nd_block = 256;
   cudaError_t r = cudaStreamSynchronize(x->stream);
   if (r != cudaSuccess) {
     bl_finalize(x);
@@ -1391,7 +1392,7 @@ int bl_run_batch(bl_ctx* x, bl_timestep* ts, int max_steps, int* status, int* ns
   cudaMemcpyAsync(x->F.steps, x->hsteps, sizeof(DevStep) * n, cudaMemcpyHostToDevice, x->stream);
   if (max_steps == 0) return bl_synchronize(x) == 0 ? BL_SUCCESS : BL_FAILURE;
   const bool with_ale = x->c.ale_zexist != 0;
-  const int G = 16;  // steps per graph launch
+  const int G = x->b_graph_steps;  // steps per graph launch
   cudaError_t r;
   bl::DevFields F = x->F;
   F.hist = nullptr;
@@ -1404,7 +1405,7 @@ int bl_run_batch(bl_ctx* x, bl_timestep* ts, int max_steps, int* status, int* ns
     x->L.lag_state_b(F, C, x->stream);
     if (with_ale) x->L.ale_b(F, C, x->stream);
   };
-  if (!x->bexec || x->b_ale != with_ale) {
+  if (!x->bexec || x->b_ale != with_ale || x->b_gsteps != G || x->b_ndblock != F.nd_block) {
     if (x->bexec) cudaGraphExecDestroy(x->bexec);
     x->bexec = nullptr;
     cudaGraph_t g;
@@ -1420,6 +1421,8 @@ int bl_run_batch(bl_ctx* x, bl_timestep* ts, int max_steps, int* status, int* ns
       return cuda_fail(e, r, "bl_run_batch instantiate");
     }
     x->b_ale = with_ale;
+    x->b_gsteps = G;
+    x->b_ndblock = F.nd_block;
   }
   const int per_step = bl::kLaunchesGetdt + bl::kLaunchesLagstep + (with_ale ? bl::kLaunchesAle : 0);
   int done = 0;
@@ -1475,5 +1478,63 @@ int bl_run_batch(bl_ctx* x, bl_timestep* ts, int max_steps, int* status, int* ns
 }
 
 int bl_batch_size(bl_ctx* x) { return x ? x->ninst : 0; }
+
+// The batch's autotuner: steps per graph G in {8, 16, 32} and the node
+// kernels' block size in {128, 256, 512}, each candidate timed (CUDA
+// events on the context's stream, host polling included) over the same 32
+// steps from the state held by the meshes' registered host arrays, after one
+// untimed graph that instantiates it; the state is uploaded again before
+// every run and after the last.
+int bl_autotune_batch(bl_ctx* x, const bl_timestep* ts, int* graph_steps, int* node_block,
+                      double* ms_per_step, int n_ms, bl_error* e) {
+  set_err(e, BL_SUCCESS, BL_HALT_SINGLE, "");
+  if (!x || !ts || x->ninst < 1) {
+    set_err(e, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_autotune_batch: bad argument (or not a batch)");
+    return BL_FAILURE;
+  }
+  static const int kG[3] = {8, 16, 32}, kB[3] = {128, 256, 512};
+  const int n = x->ninst;
+  std::vector<bl_timestep> tsc(n);
+  cudaEvent_t a, b;
+  if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess)
+    return cuda_fail(e, cudaErrorMemoryAllocation, "bl_autotune_batch");
+  double best = 1e300;
+  int bg = 16, bb = 256, k = 0, rc = BL_SUCCESS;
+  for (int gi = 0; gi < 3 && rc == BL_SUCCESS; gi++)
+    for (int bi = 0; bi < 3 && rc == BL_SUCCESS; bi++, k++) {
+      x->b_graph_steps = kG[gi];
+      x->F.nd_block = kB[bi];
+      float t = 0.0f;
+      for (int pass = 0; pass < 2 && rc == BL_SUCCESS; pass++) {
+        rc = bl_sync_to_device(x, 0);
+        if (rc != BL_SUCCESS) break;
+        tsc.assign(ts, ts + n);
+        int ns = 0;
+        if (pass == 1) cudaEventRecord(a, x->stream);
+        rc = bl_run_batch(x, tsc.data(), pass == 0 ? kG[gi] : 32, nullptr, &ns, e);
+        if (pass == 1) {
+          cudaEventRecord(b, x->stream);
+          cudaEventSynchronize(b);
+          cudaEventElapsedTime(&t, a, b);
+          t /= (float)std::max(1, ns);
+        }
+      }
+      if (rc != BL_SUCCESS) break;
+      if (ms_per_step && k < n_ms) ms_per_step[k] = t;
+      if (t < best) {
+        best = t;
+        bg = kG[gi];
+        bb = kB[bi];
+      }
+    }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  x->b_graph_steps = bg;
+  x->F.nd_block = bb;
+  if (rc == BL_SUCCESS) rc = bl_sync_to_device(x, 0);
+  if (graph_steps) *graph_steps = bg;
+  if (node_block) *node_block = bb;
+  return rc;
+}
 
 }  // extern "C"

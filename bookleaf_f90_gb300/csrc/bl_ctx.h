@@ -42,6 +42,8 @@ struct bl_ctx {
   std::vector<std::vector<char>> bstore;       // the concatenated host arrays, by field
   cudaGraphExec_t bexec = nullptr;             // graph of batch steps
   bool b_ale = false;
+  int b_graph_steps = 16;                      // steps per graph (autotuned)
+  int b_gsteps = 0, b_ndblock = 0;             // what bexec was captured with
   // bl_run
   cudaGraphExec_t gexec = nullptr;
   int gsteps = 0;

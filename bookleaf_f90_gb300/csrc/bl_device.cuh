@@ -128,6 +128,7 @@ struct DevFields {
   const int* ndinst;         // [nnd] mesh of a node
   const int* blkinst;        // [nblk_batch] mesh of a k_getdt block
   int ninst, nblk_batch;
+  int nd_block;              // block size of the batch's node kernels (autotuned)
 };
 
 // ---------------------------------------------------------------- helpers

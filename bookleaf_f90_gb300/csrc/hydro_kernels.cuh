@@ -1467,7 +1467,10 @@ void launch_lag_force_batch(const DevFields& F, const DevCfg& C, cudaStream_t s)
   k_lag_force<BS_EL, true><<<(F.nel + BS_EL - 1) / BS_EL, BS_EL, 0, s>>>(F, C);
 }
 void launch_lag_accel_batch(const DevFields& F, const DevCfg& C, cudaStream_t s) {
-  k_lag_accel<BS_ND, true><<<(F.nnd + BS_ND - 1) / BS_ND, BS_ND, 0, s>>>(F, C);
+  // block size chosen by the batch's autotuner (128, 256 or 512)
+  if (F.nd_block == 128) k_lag_accel<128, true><<<(F.nnd + 127) / 128, 128, 0, s>>>(F, C);
+  else if (F.nd_block == 512) k_lag_accel<512, true><<<(F.nnd + 511) / 512, 512, 0, s>>>(F, C);
+  else k_lag_accel<256, true><<<(F.nnd + 255) / 256, 256, 0, s>>>(F, C);
 }
 void launch_lag_state_batch(const DevFields& F, const DevCfg& C, cudaStream_t s) {
   k_lag_state<BS_EL, true><<<(F.nel + BS_EL - 1) / BS_EL, BS_EL, 0, s>>>(F, C);

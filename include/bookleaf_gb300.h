@@ -224,6 +224,16 @@ int bl_run_batch(bl_ctx *ctx, bl_timestep *ts, int max_steps, int *status, int *
                  bl_error *err);
 /* Number of meshes of a batch context (0 for a single mesh). */
 int bl_batch_size(bl_ctx *ctx);
+/* The batch's autotuner: times each candidate of the steps per graph (8, 16,
+ * 32) and the block size of the node kernels (128, 256, 512) over the same
+ * 32 steps from ts, keeps the fastest for the following bl_run_batch calls
+ * and reports it.  It runs from the state in the meshes' registered host
+ * arrays and uploads that state again when done, so call it when those
+ * arrays hold the state to run from (after bl_init_batch, or after
+ * bl_sync_to_host).  ms_per_step[0..8] (may be NULL) receives each
+ * candidate's time per step, G-major. */
+int bl_autotune_batch(bl_ctx *ctx, const bl_timestep *ts, int *graph_steps, int *node_block,
+                      double *ms_per_step, int n_ms, bl_error *err);
 
 /* ---- introspection ------------------------------------------------------- */
 

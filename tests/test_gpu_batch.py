@@ -105,3 +105,21 @@ def test_batch_rejects_different_settings_and_single_mesh_calls():
     assert b.L.bl_getdt(b.ctx, ct.byref(ts), ct.byref(err)) == abi.FAILURE
     assert "batch context" in err.message
     b.close()
+
+
+def test_autotuned_batch_still_equals_each_mesh_alone():
+    """The autotuner runs candidates from the registered host arrays and
+    uploads them again: the run after it is unchanged, bit for bit."""
+    probs = [Problem.from_deck(d) for d in EULERIAN]
+    b = BatchSolver(probs, fp_mode=abi.FP_EXACT)
+    g, bs, ms = b.autotune()
+    assert g in (8, 16, 32) and bs in (128, 256, 512)
+    assert all(v > 0.0 for v in ms.values()) and ms[(g, bs)] == min(ms.values())
+    ierr, status, _ = b.run()
+    assert ierr == 0, b.error.message
+    b.sync_to_host(0)
+    for d, p in zip(EULERIAN, probs):
+        _, q = _alone(d, abi.FP_EXACT)
+        assert _same_timestep(p.timestep, q.timestep)
+        assert not compare(p, q, exact=True)
+    b.close()
