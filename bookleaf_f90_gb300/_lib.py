@@ -64,6 +64,19 @@ def load(build_if_missing=True):
     L.bl_autotune_batch.argtypes = [vp, vp, P(ct.c_int), P(ct.c_int), P(ct.c_double), ct.c_int,
                                     P(abi.Error)]
     L.bl_autotune_batch.restype = ct.c_int
+    L.bl_mlp_create.argtypes = [P(vp), vp]
+    L.bl_mlp_create.restype = ct.c_int
+    L.bl_mlp_destroy.argtypes = [vp]
+    L.bl_mlp_destroy.restype = ct.c_int
+    L.bl_mlp_params.argtypes = [vp, vp]
+    L.bl_mlp_params.restype = ct.c_int
+    L.bl_mlp_predict.argtypes = [vp, vp, ct.c_int, vp]
+    L.bl_mlp_predict.restype = ct.c_int
+    L.bl_mlp_gradient.argtypes = [vp, vp, vp, ct.c_int, vp, P(ct.c_float)]
+    L.bl_mlp_gradient.restype = ct.c_int
+    L.bl_mlp_train.argtypes = [vp, vp, vp, ct.c_int, ct.c_int, ct.c_int, ct.c_float,
+                               ct.c_ulonglong, vp]
+    L.bl_mlp_train.restype = ct.c_int
     L.bl_fp64_rates.restype = ct.c_int
     L.bl_shortprint.argtypes = [vp, ct.c_int, P(ct.c_double), ct.c_int, P(abi.Error)]
     L.bl_shortprint.restype = ct.c_int
@@ -80,7 +93,9 @@ EXPORTS = ("bl_init", "bl_finalize", "bl_getdt", "bl_lagstep", "bl_alestep", "bl
            "bl_sync_to_host", "bl_sync_to_device", "bl_synchronize", "bl_stream",
            "bl_kernel_launches", "bl_version", "bl_getdt_noalloc", "bl_selftest_fp64",
            "bl_fp64_rates", "bl_shortprint", "bl_check_sod", "bl_time_step_kernels",
-           "bl_init_batch", "bl_run_batch", "bl_batch_size", "bl_autotune_batch")
+           "bl_init_batch", "bl_run_batch", "bl_batch_size", "bl_autotune_batch",
+           "bl_mlp_create", "bl_mlp_destroy", "bl_mlp_params", "bl_mlp_predict",
+           "bl_mlp_gradient", "bl_mlp_train")
 
 
 def fp64_rates():

@@ -1,6 +1,6 @@
 """Build the sm_103a shared library libbookleaf_gb300.so in-tree.
 
-Six translation units, compiled in parallel with nvcc:
+Seven translation units, compiled in parallel with nvcc:
   bl_kernels.cu  -DBL_NS=fast  --fmad=true   (fused multiply-add and exact
                  -DBL_FAST_ALGEBRA=1          algebraic identities allowed)
   bl_kernels.cu  -DBL_NS=exact --fmad=false  (bit-reproducible path)
@@ -8,6 +8,7 @@ Six translation units, compiled in parallel with nvcc:
   bl_noalloc.cu                               (allocation-free getdt)
   bl_selftest.cu                              (FP64 self-test and rates)
   bl_diag.cu     --fmad=false                 (short print, Sod check)
+  bl_mlp.cu                                   (the closure network, tensor cores)
 and linked with the CUDA runtime statically, so the library needs nothing
 but the driver at run time.
 
@@ -68,6 +69,7 @@ def build(force=False, verbose=False, extra=()):
         (common + ["-c", os.path.join(CSRC, "bl_selftest.cu"), "-o", os.path.join(BUILD, "selftest.o")]),
         (common + ["--fmad=false", "-c", os.path.join(CSRC, "bl_diag.cu"),
                    "-o", os.path.join(BUILD, "diag.o")]),
+        (common + ["-c", os.path.join(CSRC, "bl_mlp.cu"), "-o", os.path.join(BUILD, "mlp.o")]),
     ]
     cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
     for name in HOST_SOURCES:
@@ -88,7 +90,8 @@ def build(force=False, verbose=False, extra=()):
                                          os.path.join(BUILD, "capi.o"),
                                          os.path.join(BUILD, "noalloc.o"),
                                          os.path.join(BUILD, "selftest.o"),
-                                         os.path.join(BUILD, "diag.o")])
+                                         os.path.join(BUILD, "diag.o"),
+                                         os.path.join(BUILD, "mlp.o")])
     os.replace(tmp, LIB)
     tmp = EXE + ".%d.tmp" % os.getpid()
     subprocess.check_call([cxx, "-o", tmp] + [os.path.join(BUILD, "h_" + n + ".o") for n in HOST_SOURCES]

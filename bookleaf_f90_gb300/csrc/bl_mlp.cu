@@ -1,0 +1,495 @@
+// bl_mlp.cu -- the learned mixed-cell closure's network: 10 inputs, two
+// hidden layers of 64 with SiLU, 2 outputs, trained and evaluated on the
+// tensor cores (BF16 operands, FP32 accumulation) by the kernels below.
+//
+//   z1 = W1 x + b1, h1 = silu(z1), z2 = W2 h1 + b2, h2 = silu(z2),
+//   y = W3 h2 + b3,  loss = sum over samples and outputs of (y - t)^2 / (2 n)
+//
+// Every product of the forward and backward passes is a 16x8x16 tile
+// product (mma.sync m16n8k16, BF16 x BF16 -> FP32) of 16 samples per warp:
+// the activations and weights are rounded to BF16 where they enter a
+// product, everything else (biases, SiLU, sums, Adam) stays FP32.  The
+// weight gradients of a block of 64 samples are summed on the tensor cores
+// too (the sample dimension is the product's k), then over blocks in a
+// fixed order, so training is deterministic.  Parameters are FP32 master
+// copies in one array (layout below); no CPU path exists.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "../../include/bookleaf_gb300.h"
+
+namespace {
+
+constexpr int NI = BL_MLP_IN, NH = BL_MLP_HIDDEN, NO = BL_MLP_OUT;
+// parameter layout: W1[NH][NI], b1[NH], W2[NH][NH], b2[NH], W3[NO][NH], b3[NO]
+constexpr int OW1 = 0, OB1 = OW1 + NH * NI, OW2 = OB1 + NH, OB2 = OW2 + NH * NH,
+              OW3 = OB2 + NH, OB3 = OW3 + NO * NH, NP = OB3 + NO;
+static_assert(NP == BL_MLP_NPARAM, "parameter count");
+constexpr int WARPS = 4, TPB = 32 * WARPS, SPB = 16 * WARPS;  // samples per block
+
+__device__ __forceinline__ uint32_t pack(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  uint32_t u;
+  memcpy(&u, &v, 4);
+  return u;
+}
+
+// D = A(16x16, row) * B(16x8, col) + D, BF16 operands, FP32 accumulators
+__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4],
+                                         const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// Fragments of a 16x16 A tile and a 16x8 B tile read through accessors
+// a(row, col) and b(k, n); the accumulator element c[i] of a lane is at row
+// g + 8*(i/2), column 2t + (i%2) (g = lane/4, t = lane%4).
+template <class FA>
+__device__ __forceinline__ void frag_a(uint32_t (&r)[4], FA a) {
+  const int l = threadIdx.x & 31, g = l >> 2, t = l & 3;
+  r[0] = pack(a(g, 2 * t), a(g, 2 * t + 1));
+  r[1] = pack(a(g + 8, 2 * t), a(g + 8, 2 * t + 1));
+  r[2] = pack(a(g, 2 * t + 8), a(g, 2 * t + 9));
+  r[3] = pack(a(g + 8, 2 * t + 8), a(g + 8, 2 * t + 9));
+}
+template <class FB>
+__device__ __forceinline__ void frag_b(uint32_t (&r)[2], FB b) {
+  const int l = threadIdx.x & 31, g = l >> 2, t = l & 3;
+  r[0] = pack(b(2 * t, g), b(2 * t + 1, g));
+  r[1] = pack(b(2 * t + 8, g), b(2 * t + 9, g));
+}
+template <class FS>
+__device__ __forceinline__ void store_c(const float (&c)[4], FS s) {
+  const int l = threadIdx.x & 31, g = l >> 2, t = l & 3;
+  s(g, 2 * t, c[0]);
+  s(g, 2 * t + 1, c[1]);
+  s(g + 8, 2 * t, c[2]);
+  s(g + 8, 2 * t + 1, c[3]);
+}
+
+__device__ __forceinline__ float sigm(float z) { return 1.0f / (1.0f + __expf(-z)); }
+
+// The parameters in shared memory, zero-padded to whole tiles: W1 as 64x16,
+// W3 as 16x64.
+struct SmemW {
+  float w1[NH][16], b1[NH], w2[NH][NH], b2[NH], w3[16][NH], b3[16];
+};
+__device__ void load_weights(SmemW& w, const float* P) {
+  for (int i = threadIdx.x; i < NH * 16; i += blockDim.x) {
+    const int r = i / 16, c = i % 16;
+    w.w1[r][c] = c < NI ? P[OW1 + r * NI + c] : 0.0f;
+  }
+  for (int i = threadIdx.x; i < NH * NH; i += blockDim.x) w.w2[i / NH][i % NH] = P[OW2 + i];
+  for (int i = threadIdx.x; i < 16 * NH; i += blockDim.x) {
+    const int r = i / NH, c = i % NH;
+    w.w3[r][c] = r < NO ? P[OW3 + r * NH + c] : 0.0f;
+  }
+  for (int i = threadIdx.x; i < NH; i += blockDim.x) {
+    w.b1[i] = P[OB1 + i];
+    w.b2[i] = P[OB2 + i];
+  }
+  for (int i = threadIdx.x; i < 16; i += blockDim.x) w.b3[i] = i < NO ? P[OB3 + i] : 0.0f;
+}
+
+// One warp's 16 samples: x (16x16, padded), pre-activations and activations
+struct SmemS {
+  float x[16][16], z1[16][NH], h1[16][NH], z2[16][NH], h2[16][NH], y[16][16];
+};
+
+// Forward pass of a warp's samples (rows of s.x) into s.z1 ... s.y
+__device__ void forward_warp(const SmemW& w, SmemS& s) {
+  // layer 1: z1 = x W1^T + b1 (K = 16 padded inputs, N = 64)
+  uint32_t a[4];
+  frag_a(a, [&](int r, int c) { return s.x[r][c]; });
+#pragma unroll
+  for (int nt = 0; nt < NH / 8; nt++) {
+    float d[4] = {0, 0, 0, 0};
+    uint32_t b[2];
+    frag_b(b, [&](int k, int n) { return w.w1[nt * 8 + n][k]; });
+    mma16816(d, a, b);
+    store_c(d, [&](int r, int c, float v) { s.z1[r][nt * 8 + c] = v + w.b1[nt * 8 + c]; });
+  }
+  __syncwarp();
+  for (int i = threadIdx.x & 31; i < 16 * NH; i += 32) {
+    const float z = s.z1[i / NH][i % NH];
+    s.h1[i / NH][i % NH] = z * sigm(z);
+  }
+  __syncwarp();
+  // layer 2: z2 = h1 W2^T + b2 (K = 64, N = 64)
+#pragma unroll
+  for (int nt = 0; nt < NH / 8; nt++) {
+    float d[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int kt = 0; kt < NH / 16; kt++) {
+      frag_a(a, [&](int r, int c) { return s.h1[r][kt * 16 + c]; });
+      uint32_t b[2];
+      frag_b(b, [&](int k, int n) { return w.w2[nt * 8 + n][kt * 16 + k]; });
+      mma16816(d, a, b);
+    }
+    store_c(d, [&](int r, int c, float v) { s.z2[r][nt * 8 + c] = v + w.b2[nt * 8 + c]; });
+  }
+  __syncwarp();
+  for (int i = threadIdx.x & 31; i < 16 * NH; i += 32) {
+    const float z = s.z2[i / NH][i % NH];
+    s.h2[i / NH][i % NH] = z * sigm(z);
+  }
+  __syncwarp();
+  // layer 3: y = h2 W3^T + b3 (K = 64, N = 8 of which NO used)
+  float d[4] = {0, 0, 0, 0};
+#pragma unroll
+  for (int kt = 0; kt < NH / 16; kt++) {
+    frag_a(a, [&](int r, int c) { return s.h2[r][kt * 16 + c]; });
+    uint32_t b[2];
+    frag_b(b, [&](int k, int n) { return w.w3[n][kt * 16 + k]; });
+    mma16816(d, a, b);
+  }
+  store_c(d, [&](int r, int c, float v) { s.y[r][c] = v + w.b3[c]; });
+  __syncwarp();
+}
+
+__device__ void load_x(SmemS& s, const float* X, int base, int n) {
+  for (int i = threadIdx.x & 31; i < 16 * 16; i += 32) {
+    const int r = i / 16, c = i % 16, row = base + r;
+    s.x[r][c] = (c < NI && row < n) ? X[(size_t)row * NI + c] : 0.0f;
+  }
+  __syncwarp();
+}
+
+__global__ void __launch_bounds__(TPB) k_mlp_forward(const float* P, const float* X, float* Y,
+                                                     int n) {
+  extern __shared__ unsigned char smem[];
+  SmemW& w = *reinterpret_cast<SmemW*>(smem);
+  SmemS* S = reinterpret_cast<SmemS*>(smem + sizeof(SmemW));
+  load_weights(w, P);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5;
+  SmemS& s = S[warp];
+  const int base = blockIdx.x * SPB + warp * 16;
+  load_x(s, X, base, n);
+  forward_warp(w, s);
+  for (int i = threadIdx.x & 31; i < 16 * NO; i += 32) {
+    const int r = i / NO, c = i % NO;
+    if (base + r < n) Y[(size_t)(base + r) * NO + c] = s.y[r][c];
+  }
+}
+
+// Forward and backward of one block's 64 samples; the block's gradient sum
+// and loss sum go to G[blockIdx][NP] and L[blockIdx].
+__global__ void __launch_bounds__(TPB) k_mlp_grad(const float* P, const float* X, const float* T,
+                                                  const int* idx, int n, float inv_n, float* G,
+                                                  float* L) {
+  extern __shared__ unsigned char smem[];
+  SmemW& w = *reinterpret_cast<SmemW*>(smem);
+  SmemS* S = reinterpret_cast<SmemS*>(smem + sizeof(SmemW));
+  // per block: dz1, dz2 (64 samples x 64), dy (64 x 16), gathered x (64 x 16)
+  float(*dz1)[NH] = reinterpret_cast<float(*)[NH]>(smem + sizeof(SmemW) + WARPS * sizeof(SmemS));
+  float(*dz2)[NH] = dz1 + SPB;
+  float(*dy)[16] = reinterpret_cast<float(*)[16]>(dz2 + SPB);
+  float* lsum = reinterpret_cast<float*>(dy + SPB);
+  load_weights(w, P);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x < WARPS) lsum[threadIdx.x] = 0.0f;
+  __syncthreads();
+  SmemS& s = S[warp];
+  const int base = blockIdx.x * SPB + warp * 16;
+  // the samples of this warp (through the permutation idx, if given)
+  for (int i = lane; i < 16 * 16; i += 32) {
+    const int r = i / 16, c = i % 16, row = base + r;
+    const int src = row < n ? (idx ? idx[row] : row) : -1;
+    s.x[r][c] = (c < NI && src >= 0) ? X[(size_t)src * NI + c] : 0.0f;
+  }
+  __syncwarp();
+  forward_warp(w, s);
+  // dy = (y - t) / n for valid samples; loss terms
+  float lp = 0.0f;
+  for (int i = lane; i < 16 * 16; i += 32) {
+    const int r = i / 16, c = i % 16, row = base + r;
+    float g = 0.0f;
+    if (c < NO && row < n) {
+      const int src = idx ? idx[row] : row;
+      const float e = s.y[r][c] - T[(size_t)src * NO + c];
+      lp += e * e;
+      g = e * inv_n;
+    }
+    dy[warp * 16 + r][c] = g;
+  }
+  for (int o = 16; o > 0; o >>= 1) lp += __shfl_xor_sync(0xffffffffu, lp, o);
+  if (lane == 0) lsum[warp] = lp;
+  __syncwarp();
+  const int row0 = warp * 16;
+  // dh2 = dy W3 (K = 16 padded outputs, N = 64); dz2 = dh2 silu'(z2)
+  uint32_t a[4];
+  frag_a(a, [&](int r, int c) { return dy[row0 + r][c]; });
+#pragma unroll
+  for (int nt = 0; nt < NH / 8; nt++) {
+    float d[4] = {0, 0, 0, 0};
+    uint32_t b[2];
+    frag_b(b, [&](int k, int nn) { return w.w3[k][nt * 8 + nn]; });
+    mma16816(d, a, b);
+    store_c(d, [&](int r, int c, float v) {
+      const float z = s.z2[r][nt * 8 + c], sg = sigm(z);
+      dz2[row0 + r][nt * 8 + c] = v * sg * (1.0f + z * (1.0f - sg));
+    });
+  }
+  __syncwarp();
+  // dh1 = dz2 W2 (K = 64, N = 64); dz1 = dh1 silu'(z1)
+#pragma unroll
+  for (int nt = 0; nt < NH / 8; nt++) {
+    float d[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int kt = 0; kt < NH / 16; kt++) {
+      frag_a(a, [&](int r, int c) { return dz2[row0 + r][kt * 16 + c]; });
+      uint32_t b[2];
+      frag_b(b, [&](int k, int nn) { return w.w2[kt * 16 + k][nt * 8 + nn]; });
+      mma16816(d, a, b);
+    }
+    store_c(d, [&](int r, int c, float v) {
+      const float z = s.z1[r][nt * 8 + c], sg = sigm(z);
+      dz1[row0 + r][nt * 8 + c] = v * sg * (1.0f + z * (1.0f - sg));
+    });
+  }
+  __syncthreads();
+  // Weight gradients summed over the block's 64 samples (the k of the
+  // products): dW = dZ^T A with A the layer's input activations.  Warp w
+  // takes the output rows [16w, 16w + 16) of dW1 and dW2 and, for dW3, the
+  // columns [16w, 16w + 16).
+  float* Gb = G + (size_t)blockIdx.x * NP;
+  // dW2[o][i] = sum_s dz2[s][o] h1[s][i]; dW1[o][i] = sum_s dz1[s][o] x[s][i]
+  for (int layer = 0; layer < 2; layer++) {
+    const int ncols = layer == 0 ? NH : 16;
+    for (int nt = 0; nt < ncols / 8; nt++) {
+      float d[4] = {0, 0, 0, 0};
+      for (int kt = 0; kt < SPB / 16; kt++) {   // 16 samples of warp kt
+        SmemS& sk = S[kt];
+        frag_a(a, [&](int r, int c) {
+          return layer == 0 ? dz2[kt * 16 + c][warp * 16 + r] : dz1[kt * 16 + c][warp * 16 + r];
+        });
+        uint32_t b[2];
+        frag_b(b, [&](int k, int nn) {
+          return layer == 0 ? sk.h1[k][nt * 8 + nn] : sk.x[k][nt * 8 + nn];
+        });
+        mma16816(d, a, b);
+      }
+      store_c(d, [&](int r, int c, float v) {
+        const int o = warp * 16 + r, i = nt * 8 + c;
+        if (layer == 0) Gb[OW2 + o * NH + i] = v;
+        else if (i < NI) Gb[OW1 + o * NI + i] = v;
+      });
+    }
+  }
+  // dW3[o][i] = sum_s dy[s][o] h2[s][i] (o < NO of 16 padded rows)
+  for (int nt = 0; nt < 2; nt++) {
+    float d[4] = {0, 0, 0, 0};
+    for (int kt = 0; kt < SPB / 16; kt++) {
+      SmemS& sk = S[kt];
+      frag_a(a, [&](int r, int c) { return dy[kt * 16 + c][r]; });
+      uint32_t b[2];
+      frag_b(b, [&](int k, int nn) { return sk.h2[k][warp * 16 + nt * 8 + nn]; });
+      mma16816(d, a, b);
+    }
+    store_c(d, [&](int r, int c, float v) {
+      if (r < NO) Gb[OW3 + r * NH + warp * 16 + nt * 8 + c] = v;
+    });
+  }
+  // bias gradients: column sums over the block's samples (FP32)
+  for (int i = threadIdx.x; i < NH; i += blockDim.x) {
+    float g1 = 0.0f, g2 = 0.0f;
+    for (int r = 0; r < SPB; r++) {
+      g1 += dz1[r][i];
+      g2 += dz2[r][i];
+    }
+    Gb[OB1 + i] = g1;
+    Gb[OB2 + i] = g2;
+  }
+  if (threadIdx.x < NO) {
+    float g3 = 0.0f;
+    for (int r = 0; r < SPB; r++) g3 += dy[r][threadIdx.x];
+    Gb[OB3 + threadIdx.x] = g3;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) L[blockIdx.x] = 0.5f * inv_n * (lsum[0] + lsum[1] + lsum[2] + lsum[3]);
+}
+
+// Sums the per-block gradients and losses in block order.
+__global__ void k_mlp_reduce(const float* G, const float* L, int nblk, float* grad, float* loss) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < NP) {
+    float s = 0.0f;
+    for (int b = 0; b < nblk; b++) s += G[(size_t)b * NP + i];
+    grad[i] = s;
+  }
+  if (i == 0) {
+    float s = 0.0f;
+    for (int b = 0; b < nblk; b++) s += L[b];
+    *loss = s;
+  }
+}
+
+// Adam on the FP32 master parameters (Kingma and Ba, 2015).
+__global__ void k_mlp_adam(float* P, float* M, float* V, const float* grad, float lr, float b1,
+                           float b2, float eps, float c1, float c2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= NP) return;
+  const float g = grad[i];
+  const float m = b1 * M[i] + (1.0f - b1) * g, v = b2 * V[i] + (1.0f - b2) * g * g;
+  M[i] = m;
+  V[i] = v;
+  P[i] -= lr * (m * c1) / (sqrtf(v * c2) + eps);
+}
+
+constexpr size_t kSmemFwd = sizeof(SmemW) + WARPS * sizeof(SmemS);
+constexpr size_t kSmemGrad = kSmemFwd + (2 * SPB * NH + SPB * 16 + WARPS) * sizeof(float);
+
+}  // namespace
+
+struct bl_mlp {
+  float *P = nullptr, *M = nullptr, *V = nullptr, *grad = nullptr, *loss = nullptr;
+  int step = 0;
+};
+
+extern "C" {
+
+int bl_mlp_create(bl_mlp** out, const float* params) {
+  if (!out || !params) return BL_FAILURE;
+  *out = nullptr;
+  bl_mlp* m = new bl_mlp();
+  bool ok = cudaMalloc(&m->P, NP * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&m->M, NP * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&m->V, NP * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&m->grad, NP * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&m->loss, sizeof(float)) == cudaSuccess;
+  ok = ok && cudaMemcpy(m->P, params, NP * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemset(m->M, 0, NP * sizeof(float)) == cudaSuccess &&
+       cudaMemset(m->V, 0, NP * sizeof(float)) == cudaSuccess;
+  ok = ok && cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kSmemFwd) == cudaSuccess &&
+       cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)kSmemGrad) == cudaSuccess;
+  if (!ok) {
+    bl_mlp_destroy(m);
+    return BL_FAILURE;
+  }
+  *out = m;
+  return BL_SUCCESS;
+}
+
+int bl_mlp_destroy(bl_mlp* m) {
+  if (!m) return BL_SUCCESS;
+  cudaFree(m->P);
+  cudaFree(m->M);
+  cudaFree(m->V);
+  cudaFree(m->grad);
+  cudaFree(m->loss);
+  delete m;
+  return BL_SUCCESS;
+}
+
+int bl_mlp_params(bl_mlp* m, float* params) {
+  if (!m || !params) return BL_FAILURE;
+  return cudaMemcpy(params, m->P, NP * sizeof(float), cudaMemcpyDeviceToHost) == cudaSuccess
+             ? BL_SUCCESS : BL_FAILURE;
+}
+
+const float* bl_mlp_device_params(bl_mlp* m) { return m ? m->P : nullptr; }
+
+int bl_mlp_predict(bl_mlp* m, const float* x, int n, float* y) {
+  if (!m || !x || !y || n < 0) return BL_FAILURE;
+  if (n == 0) return BL_SUCCESS;
+  float *dx = nullptr, *dy = nullptr;
+  bool ok = cudaMalloc(&dx, (size_t)n * NI * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&dy, (size_t)n * NO * sizeof(float)) == cudaSuccess;
+  ok = ok && cudaMemcpy(dx, x, (size_t)n * NI * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
+  if (ok) {
+    k_mlp_forward<<<(n + SPB - 1) / SPB, TPB, kSmemFwd>>>(m->P, dx, dy, n);
+    ok = cudaMemcpy(y, dy, (size_t)n * NO * sizeof(float), cudaMemcpyDeviceToHost) == cudaSuccess;
+  }
+  cudaFree(dx);
+  cudaFree(dy);
+  return ok ? BL_SUCCESS : BL_FAILURE;
+}
+
+int bl_mlp_gradient(bl_mlp* m, const float* x, const float* t, int n, float* grad, float* loss) {
+  if (!m || !x || !t || !grad || n < 1) return BL_FAILURE;
+  const int nblk = (n + SPB - 1) / SPB;
+  float *dx = nullptr, *dt = nullptr, *G = nullptr, *L = nullptr;
+  bool ok = cudaMalloc(&dx, (size_t)n * NI * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&dt, (size_t)n * NO * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&G, (size_t)nblk * NP * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&L, (size_t)nblk * sizeof(float)) == cudaSuccess;
+  ok = ok && cudaMemcpy(dx, x, (size_t)n * NI * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(dt, t, (size_t)n * NO * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
+  if (ok) {
+    k_mlp_grad<<<nblk, TPB, kSmemGrad>>>(m->P, dx, dt, nullptr, n, 1.0f / (float)n, G, L);
+    k_mlp_reduce<<<(NP + 255) / 256, 256>>>(G, L, nblk, m->grad, m->loss);
+    ok = cudaMemcpy(grad, m->grad, NP * sizeof(float), cudaMemcpyDeviceToHost) == cudaSuccess;
+    if (ok && loss) ok = cudaMemcpy(loss, m->loss, sizeof(float), cudaMemcpyDeviceToHost) == cudaSuccess;
+  }
+  cudaFree(dx);
+  cudaFree(dt);
+  cudaFree(G);
+  cudaFree(L);
+  return ok ? BL_SUCCESS : BL_FAILURE;
+}
+
+int bl_mlp_train(bl_mlp* m, const float* x, const float* t, int n, int epochs, int batch,
+                 float lr, unsigned long long seed, float* losses) {
+  if (!m || !x || !t || n < 1 || epochs < 1 || batch < SPB) return BL_FAILURE;
+  const int nb_per = (batch + SPB - 1) / SPB;
+  float *dx = nullptr, *dt = nullptr, *G = nullptr, *L = nullptr;
+  int* didx = nullptr;
+  bool ok = cudaMalloc(&dx, (size_t)n * NI * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&dt, (size_t)n * NO * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&didx, (size_t)n * sizeof(int)) == cudaSuccess &&
+            cudaMalloc(&G, (size_t)nb_per * NP * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&L, (size_t)nb_per * sizeof(float)) == cudaSuccess;
+  ok = ok && cudaMemcpy(dx, x, (size_t)n * NI * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(dt, t, (size_t)n * NO * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
+  std::vector<int> perm(n);
+  for (int i = 0; i < n; i++) perm[i] = i;
+  uint64_t r = seed * 0x9E3779B97F4A7C15ull + 1;
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  for (int ep = 0; ep < epochs && ok; ep++) {
+    // Fisher-Yates shuffle with a splitmix-style generator
+    for (int i = n - 1; i > 0; i--) {
+      r += 0x9E3779B97F4A7C15ull;
+      uint64_t z = r;
+      z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+      z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+      z ^= z >> 31;
+      const int j = (int)(z % (uint64_t)(i + 1));
+      std::swap(perm[i], perm[j]);
+    }
+    ok = cudaMemcpy(didx, perm.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess;
+    double eloss = 0.0;
+    for (int b0 = 0; b0 < n && ok; b0 += batch) {
+      const int nb = std::min(batch, n - b0);
+      const int nblk = (nb + SPB - 1) / SPB;
+      k_mlp_grad<<<nblk, TPB, kSmemGrad>>>(m->P, dx, dt, didx + b0, nb, 1.0f / (float)nb, G, L);
+      k_mlp_reduce<<<(NP + 255) / 256, 256>>>(G, L, nblk, m->grad, m->loss);
+      m->step++;
+      const float c1 = 1.0f / (1.0f - powf(b1, (float)m->step));
+      const float c2 = 1.0f / (1.0f - powf(b2, (float)m->step));
+      k_mlp_adam<<<(NP + 255) / 256, 256>>>(m->P, m->M, m->V, m->grad, lr, b1, b2, eps, c1, c2);
+      float lb = 0.0f;
+      ok = cudaMemcpy(&lb, m->loss, sizeof(float), cudaMemcpyDeviceToHost) == cudaSuccess;
+      eloss += (double)lb * nb;
+    }
+    if (losses) losses[ep] = (float)(eloss / n);
+  }
+  ok = ok && cudaDeviceSynchronize() == cudaSuccess;
+  cudaFree(dx);
+  cudaFree(dt);
+  cudaFree(didx);
+  cudaFree(G);
+  cudaFree(L);
+  return ok ? BL_SUCCESS : BL_FAILURE;
+}
+
+}  // extern "C"

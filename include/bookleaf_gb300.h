@@ -235,6 +235,31 @@ int bl_batch_size(bl_ctx *ctx);
 int bl_autotune_batch(bl_ctx *ctx, const bl_timestep *ts, int *graph_steps, int *node_block,
                       double *ms_per_step, int n_ms, bl_error *err);
 
+/* ---- the learned mixed-cell closure's network (no counterpart in the
+ * reference) ----------------------------------------------------------------
+ * A 10 -> 64 -> 64 -> 2 MLP with SiLU, trained and evaluated on the tensor
+ * cores (BF16 operands, FP32 accumulation).  Parameters are FP32, laid out
+ * W1[64][10], b1[64], W2[64][64], b2[64], W3[2][64], b3[2].  The loss is the
+ * mean over samples of |y - t|^2 / 2.  All calls take host arrays (row per
+ * sample) and return 0, or -1 when CUDA fails. */
+#define BL_MLP_IN 10
+#define BL_MLP_HIDDEN 64
+#define BL_MLP_OUT 2
+#define BL_MLP_NPARAM 4994
+typedef struct bl_mlp bl_mlp;
+int bl_mlp_create(bl_mlp **m, const float *params);
+int bl_mlp_destroy(bl_mlp *m);
+/* the current parameters */
+int bl_mlp_params(bl_mlp *m, float *params);
+/* y[n][2] for x[n][10] */
+int bl_mlp_predict(bl_mlp *m, const float *x, int n, float *y);
+/* the loss and its gradient with respect to the parameters over all n samples */
+int bl_mlp_gradient(bl_mlp *m, const float *x, const float *t, int n, float *grad, float *loss);
+/* Adam (lr, betas 0.9 / 0.999) over shuffled mini-batches (seeded);
+ * losses[epochs] (may be NULL) receives each epoch's mean loss */
+int bl_mlp_train(bl_mlp *m, const float *x, const float *t, int n, int epochs, int batch,
+                 float lr, unsigned long long seed, float *losses);
+
 /* ---- introspection ------------------------------------------------------- */
 
 /* Waits for the context's stream.  Returns 0 or a CUDA error number. */
