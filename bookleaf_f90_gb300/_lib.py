@@ -77,6 +77,10 @@ def load(build_if_missing=True):
     L.bl_mlp_train.argtypes = [vp, vp, vp, ct.c_int, ct.c_int, ct.c_int, ct.c_float,
                                ct.c_ulonglong, vp]
     L.bl_mlp_train.restype = ct.c_int
+    L.bl_set_closure.argtypes = [vp, vp, vp, ct.c_int, P(abi.Error)]
+    L.bl_set_closure.restype = ct.c_int
+    L.bl_closure_stats.argtypes = [vp, P(ct.c_ulonglong), P(ct.c_ulonglong)]
+    L.bl_closure_stats.restype = ct.c_int
     L.bl_fp64_rates.restype = ct.c_int
     L.bl_shortprint.argtypes = [vp, ct.c_int, P(ct.c_double), ct.c_int, P(abi.Error)]
     L.bl_shortprint.restype = ct.c_int
@@ -95,7 +99,7 @@ EXPORTS = ("bl_init", "bl_finalize", "bl_getdt", "bl_lagstep", "bl_alestep", "bl
            "bl_fp64_rates", "bl_shortprint", "bl_check_sod", "bl_time_step_kernels",
            "bl_init_batch", "bl_run_batch", "bl_batch_size", "bl_autotune_batch",
            "bl_mlp_create", "bl_mlp_destroy", "bl_mlp_params", "bl_mlp_predict",
-           "bl_mlp_gradient", "bl_mlp_train")
+           "bl_mlp_gradient", "bl_mlp_train", "bl_set_closure", "bl_closure_stats")
 
 
 def fp64_rates():

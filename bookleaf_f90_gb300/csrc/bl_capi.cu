@@ -30,13 +30,15 @@ const bl::Launchers kFast = {bl::fast::getdt_blocks,          bl::fast::launch_g
                              bl::fast::launch_lag_state,       bl::fast::launch_ale,
                              bl::fast::launch_getdt_batch,     bl::fast::launch_lag_force_batch,
                              bl::fast::launch_lag_accel_batch, bl::fast::launch_lag_state_batch,
-                             bl::fast::launch_ale_batch};
+                             bl::fast::launch_ale_batch,       bl::fast::prepare_mix_closure,
+                             bl::fast::launch_mix_closure};
 const bl::Launchers kExact = {bl::exact::getdt_blocks,          bl::exact::launch_getdt,
                               bl::exact::launch_lag_force,       bl::exact::launch_lag_accel,
                               bl::exact::launch_lag_state,       bl::exact::launch_ale,
                               bl::exact::launch_getdt_batch,     bl::exact::launch_lag_force_batch,
                               bl::exact::launch_lag_accel_batch, bl::exact::launch_lag_state_batch,
-                              bl::exact::launch_ale_batch};
+                              bl::exact::launch_ale_batch,       bl::exact::prepare_mix_closure,
+                              bl::exact::launch_mix_closure};
 
 // batches (defined with bl_init_batch below)
 void batch_copy(bl_ctx* x, int id, bool to_mesh);
@@ -178,6 +180,7 @@ void queue_call_kernels(bl_ctx* x, int which) {
     x->L.lag_force(x->F, x->C, x->stream);
     x->L.lag_accel(x->F, x->C, x->stream);
     x->L.lag_state(x->F, x->C, x->stream);
+    x->L.mix_closure(x->F, x->C, x->stream);
   } else {
     x->L.ale(x->F, x->C, x->stream);
   }
@@ -713,7 +716,7 @@ int bl_lagstep(bl_ctx* x, bl_timestep* ts, bl_error* e) {
     return BL_FAILURE;
   }
   header_from_ts(x, ts, 0);
-  x->launches += bl::kLaunchesLagstep;
+  x->launches += bl::launches_lagstep(x->F);
   int rc = run_call(x, kCallLagstep, e, "bl_lagstep");
   if (rc != BL_SUCCESS) return rc;
   x->cs2_is_v = false;
@@ -790,6 +793,7 @@ int bl_run(bl_ctx* x, bl_timestep* ts, int max_steps, bl_step_record* history, i
       x->L.lag_force(F, C, x->stream);
       x->L.lag_accel(F, C, x->stream);
       x->L.lag_state(F, C, x->stream);
+      x->L.mix_closure(F, C, x->stream);
       if (with_ale) x->L.ale(F, C, x->stream);
     }
     r = cudaStreamEndCapture(x->stream, &g);
@@ -805,7 +809,7 @@ int bl_run(bl_ctx* x, bl_timestep* ts, int max_steps, bl_step_record* history, i
   header_from_ts(x, ts, 1);
   // step limit: getdt stops once nrecord reaches it (DevStep.nrecord counts)
   int launched = 0;
-  const int per_step = bl::kLaunchesGetdt + bl::kLaunchesLagstep + (with_ale ? bl::kLaunchesAle : 0);
+  const int per_step = bl::kLaunchesGetdt + bl::launches_lagstep(x->F) + (with_ale ? bl::kLaunchesAle : 0);
   int done = 0;
   while (true) {
     const int remaining = max_steps - done;
@@ -821,6 +825,7 @@ int bl_run(bl_ctx* x, bl_timestep* ts, int max_steps, bl_step_record* history, i
         x->L.lag_force(F, C, x->stream);
         x->L.lag_accel(F, C, x->stream);
         x->L.lag_state(F, C, x->stream);
+        x->L.mix_closure(F, C, x->stream);
         if (with_ale) x->L.ale(F, C, x->stream);
       }
       x->launches += (long long)remaining * per_step;
@@ -904,9 +909,10 @@ int bl_time_step_kernels(bl_ctx* x, bl_timestep* ts, int nstep, double* ms, int 
     x->L.lag_accel(x->F, x->C, x->stream);
     cudaEventRecord(ev[4 * k + 3], x->stream);
     x->L.lag_state(x->F, x->C, x->stream);
+    x->L.mix_closure(x->F, x->C, x->stream);
     cudaEventRecord(ev[4 * k + 4], x->stream);
   }
-  x->launches += (long long)nstep * (bl::kLaunchesGetdt + bl::kLaunchesLagstep);
+  x->launches += (long long)nstep * (bl::kLaunchesGetdt + bl::launches_lagstep(x->F));
   r = cudaEventSynchronize(ev[4 * nstep]);
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
   for (int k = 0; k < nstep && r == cudaSuccess; k++)
@@ -1424,7 +1430,7 @@ int bl_run_batch(bl_ctx* x, bl_timestep* ts, int max_steps, int* status, int* ns
     x->b_gsteps = G;
     x->b_ndblock = F.nd_block;
   }
-  const int per_step = bl::kLaunchesGetdt + bl::kLaunchesLagstep + (with_ale ? bl::kLaunchesAle : 0);
+  const int per_step = bl::kLaunchesGetdt + bl::launches_lagstep(x->F) + (with_ale ? bl::kLaunchesAle : 0);
   int done = 0;
   while (done < max_steps) {
     const int k = std::min(G, max_steps - done);
@@ -1478,6 +1484,43 @@ int bl_run_batch(bl_ctx* x, bl_timestep* ts, int max_steps, int* status, int* ns
 }
 
 int bl_batch_size(bl_ctx* x) { return x ? x->ninst : 0; }
+
+const float* bl_mlp_device_params(bl_mlp* m);  // bl_mlp.cu
+
+int bl_set_closure(bl_ctx* x, bl_mlp* net, const float* norm, int on, bl_error* e) {
+  set_err(e, BL_SUCCESS, BL_HALT_SINGLE, "");
+  if (!x || (on && (!net || !norm)) || x->ninst > 0) {
+    set_err(e, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_set_closure: bad argument (or a batch context)");
+    return BL_FAILURE;
+  }
+  bl::DevFields& F = x->F;
+  if (on) {
+    cudaError_t st = cudaSuccess;
+    if (!F.mxv0) F.mxv0 = dalloc<double>(x, std::max(1, x->s.nmx), st);
+    if (!F.mlp_norm) F.mlp_norm = dalloc<float>(x, 2 * BL_MLP_IN + 2, st);
+    if (!F.mlp_count) F.mlp_count = dalloc<unsigned long long>(x, 2, st);
+    if (st != cudaSuccess || x->L.mix_prepare() != 0) return cuda_fail(e, cudaErrorMemoryAllocation, "bl_set_closure");
+    cudaMemcpyAsync(const_cast<float*>(F.mlp_norm), norm, (2 * BL_MLP_IN + 2) * sizeof(float),
+                    cudaMemcpyHostToDevice, x->stream);
+    F.mlp_params = bl_mlp_device_params(net);
+  }
+  F.closure = on ? 1 : 0;
+  // the device loop's graph holds the old arguments
+  if (x->gexec) cudaGraphExecDestroy(x->gexec);
+  x->gexec = nullptr;
+  return cudaStreamSynchronize(x->stream) == cudaSuccess ? BL_SUCCESS : BL_FAILURE;
+}
+
+int bl_closure_stats(bl_ctx* x, unsigned long long* cells, unsigned long long* rejected) {
+  if (!x) return BL_FAILURE;
+  unsigned long long h[2] = {0, 0};
+  if (x->F.mlp_count &&
+      cudaMemcpy(h, x->F.mlp_count, sizeof h, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return BL_FAILURE;
+  if (cells) *cells = h[0];
+  if (rejected) *rejected = h[1];
+  return BL_SUCCESS;
+}
 
 // The batch's autotuner: steps per graph G in {8, 16, 32} and the node
 // kernels' block size in {128, 256, 512}, each candidate timed (CUDA

@@ -129,6 +129,12 @@ struct DevFields {
   const int* blkinst;        // [nblk_batch] mesh of a k_getdt block
   int ninst, nblk_batch;
   int nd_block;              // block size of the batch's node kernels (autotuned)
+  // learned mixed-cell closure (bl_set_closure; off when closure == 0)
+  int closure;
+  const float* mlp_params;   // the network's FP32 parameters (bl_mlp.cu layout)
+  const float* mlp_norm;     // [20]: feature means, then inverse spreads
+  double* mxv0;              // [nmx] cell volume at the start of the step
+  unsigned long long* mlp_count;  // [2]: cells the closure saw, cells it rejected
 };
 
 // ---------------------------------------------------------------- helpers

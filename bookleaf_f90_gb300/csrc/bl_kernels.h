@@ -24,6 +24,8 @@ namespace bl {
   void launch_lag_accel_batch(const DevFields& F, const DevCfg& C, cudaStream_t s);\
   void launch_lag_state_batch(const DevFields& F, const DevCfg& C, cudaStream_t s);\
   void launch_ale_batch(const DevFields& F, const DevCfg& C, cudaStream_t s);      \
+  int prepare_mix_closure();                                                       \
+  void launch_mix_closure(const DevFields& F, const DevCfg& C, cudaStream_t s);    \
   }
 
 BL_DECLARE_LAUNCHERS(fast)
@@ -42,11 +44,18 @@ struct Launchers {
   void (*lag_accel_b)(const DevFields&, const DevCfg&, cudaStream_t);
   void (*lag_state_b)(const DevFields&, const DevCfg&, cudaStream_t);
   void (*ale_b)(const DevFields&, const DevCfg&, cudaStream_t);
+  // the learned mixed-cell closure (after lag_state; no-op when off)
+  int (*mix_prepare)();
+  void (*mix_closure)(const DevFields&, const DevCfg&, cudaStream_t);
 };
 
 // Kernels launched by one call of each launcher (for bl_kernel_launches).
 constexpr int kLaunchesGetdt = 1;
 constexpr int kLaunchesLagstep = 3;
 constexpr int kLaunchesAle = 4;
+// the lagstep launcher's count with the learned closure in it
+inline int launches_lagstep(const DevFields& F) {
+  return kLaunchesLagstep + (F.closure && F.nmx > 0 ? 1 : 0);
+}
 
 }  // namespace bl

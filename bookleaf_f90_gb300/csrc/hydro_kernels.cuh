@@ -30,6 +30,7 @@
 #include "bl_device.cuh"
 #include "bl_fp64.cuh"
 #include "bl_kernels.h"
+#include "bl_mma.cuh"
 
 // Every FP64 division and square root of the path goes through the
 // integer-pipe versions, which return the IEEE results bit for bit
@@ -1401,13 +1402,18 @@ __global__ void BL_STATE_BOUNDS(BS) k_lag_state(DevFields F, DevCfg C) {
   F.b2[iel] = g.b2;
   F.b3[iel] = g.b3;
   F.cnwt[iel] = make_d4(g.w0, g.w1, g.w2, g.w3);
+  const int imx = F.elmx ? F.elmx[iel] : -1;
+  // the learned closure (k_mix_closure, launched next) splits a two-material
+  // cell's volume change between its materials and updates them: it needs
+  // the cell volume at the start of the step
+  const bool learned = imx >= 0 && F.closure && F.imxncp[imx] == 2;
+  if (learned) F.mxv0[imx] = F.vol[iel];
   F.vol[iel] = g.vol;
   F.rho[iel] = rho;
   F.e[iel] = e;
   F.p[iel] = p;
   F.cs2[iel] = cs2;
-  const int imx = F.elmx ? F.elmx[iel] : -1;
-  if (imx >= 0) {
+  if (imx >= 0 && !learned) {
     const int c0 = F.imxfcp[imx], nc = F.imxncp[imx];
     for (int k = 0; k < nc; k++) {
       const int icp = c0 + k;
@@ -1435,6 +1441,130 @@ __global__ void BL_STATE_BOUNDS(BS) k_lag_state(DevFields F, DevCfg C) {
   }
 }
 
+// ================================================================ k_mix_closure
+
+// The learned mixed-cell closure, after k_lag_state.  For each two-material
+// cell the network (tensor cores, 16 cells per warp) predicts the volume
+// each material gains over the step beyond the plain closure's share (its
+// volume fraction of the cell's change), as a fraction of the cell's volume
+// at the start: x_m = norm[20] * y_m.  Its inputs, standardised as
+// (f - norm[k]) * norm[10 + k], are the state at the start of the step:
+//   0 material 1's volume fraction, 1-2 the densities, 3-4 the pressures,
+//   5-6 the sound speeds squared, 7 dV / V^n, 8 dt sqrt(max cs2 / V^n) (a
+//   Courant number of the cell), 9 (p1 - p2) / (|p1| + |p2|).
+// The exchange used is x = (x_1 - x_2) / 2 into material 1 (x_1 + x_2 = 0
+// conserves the cell's volume), limited to the admissible range between 0
+// and x_eq, the exchange that equalises the two materials' pressures after
+// the plain closure's step (linearised with the bulk moduli rho c^2): the
+// closure may relax the materials towards pressure equilibrium, not past it.
+// The plain closure is kept in a cell whose outputs are not finite, miss
+// conservation (|y_1 + y_2| > norm[21]), lie out of range (farther than
+// |x_eq| outside [0, x_eq]) or leave a material a non-positive volume;
+// F.mlp_count[1] counts those cells.  Each material's energy takes the plain
+// closure's work, and the exchanged volume trades energy at the mixture
+// pressure fr_1 p_1 + fr_2 p_2, which sums to zero over the cell: the cell's
+// total energy, like its volume and every element and node field, is the
+// plain closure's, and a rejected cell ends exactly as under it.
+constexpr int kClosureWarps = 4;
+__global__ void __launch_bounds__(32 * kClosureWarps) k_mix_closure(DevFields F, DevCfg C) {
+  const DevStep* S = F.step;
+  if (halted(S)) return;
+  extern __shared__ unsigned char smem[];
+  mlp::SmemW& w = *reinterpret_cast<mlp::SmemW*>(smem);
+  mlp::SmemS* Ss = reinterpret_cast<mlp::SmemS*>(smem + sizeof(mlp::SmemW));
+  mlp::load_weights(w, F.mlp_params);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  mlp::SmemS& s = Ss[warp];
+  const int imx = blockIdx.x * (16 * kClosureWarps) + warp * 16 + (lane & 15);
+  const bool cell = lane < 16 && imx < F.nmx && F.imxncp[imx] == 2;
+  const double dt = S->dt;
+  double V0 = 0.0, V1 = 0.0;
+  int c0 = 0, iel = 0;
+  if (lane < 16) {
+    float f[mlp::NI];
+    if (cell) {
+      c0 = F.imxfcp[imx];
+      iel = F.imxel[imx];
+      V0 = F.mxv0[imx];
+      V1 = F.vol[iel];
+      const double p1 = F.cpp[c0], p2 = F.cpp[c0 + 1];
+      const double q1 = F.cpcs2[c0], q2 = F.cpcs2[c0 + 1];
+      const double raw[mlp::NI] = {F.frvol[c0], F.cprho[c0], F.cprho[c0 + 1], p1, p2, q1, q2,
+                                   (V1 - V0) / V0, dt * sqrt(maxF(q1, q2) / V0),
+                                   (p1 - p2) / (absF(p1) + absF(p2) + 1e-300)};
+#pragma unroll
+      for (int k = 0; k < mlp::NI; k++)
+        f[k] = ((float)raw[k] - __ldg(F.mlp_norm + k)) * __ldg(F.mlp_norm + mlp::NI + k);
+    }
+#pragma unroll
+    for (int k = 0; k < 16; k++) s.x[lane][k] = (cell && k < mlp::NI) ? f[k] : 0.0f;
+  }
+  __syncwarp();
+  mlp::forward_warp(w, s);
+  if (!cell) return;
+  const double zc = C.zerocut;
+  const double fr[2] = {F.frvol[c0], F.frvol[c0 + 1]};
+  const double pbar = fr[0] * F.cpp[c0] + fr[1] * F.cpp[c0 + 1];
+  const int4 nd = __ldg(F.ielnd + iel);
+  const int n[4] = {nd.x, nd.y, nd.z, nd.w};
+  double ub[4], vb[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    ub[j] = F.ndubar[n[j]];
+    vb[j] = F.ndvbar[n[j]];
+  }
+  // the plain closure's step (k_lag_state's component update): the
+  // fallback, and the state the admissible range is measured from
+  double pe[2], pv[2], pr[2], pp[2], pc[2];
+  for (int k = 0; k < 2; k++) {
+    const int icp = c0 + k;
+    const d4 a = F.cpfx[icp], b = F.cpfy[icp];
+    const double cfx[4] = {a.x, a.y, a.z, a.w}, cfy[4] = {b.x, b.y, b.z, b.w};
+    double cu[4], cv[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      cu[j] = fr[k] * ub[j];
+      cv[j] = fr[k] * vb[j];
+    }
+    const double cpm = F.cpm[icp];
+    pe[k] = energy_update(F.cpe[icp], cpm, zc, dt, cfx, cfy, cu, cv);
+    pv[k] = V1 * fr[k];
+    pr[k] = DIV(cpm, pv[k]);
+    eos_pc(C, __ldg(F.icpmat + icp), pr[k], pe[k], pp[k], pc[k]);
+  }
+  const double xeq = DIV((pp[0] - pp[1]) * V1,
+                         V0 * (DIV(pr[0] * pc[0], fr[0]) + DIV(pr[1] * pc[1], fr[1])));
+  const double lo = fmin(0.0, xeq), hi = fmax(0.0, xeq), m = absF(xeq);
+  const float o1 = s.y[lane][0], o2 = s.y[lane][1];
+  const double xp = 0.5 * __ldg(F.mlp_norm + 2 * mlp::NI) * ((double)o1 - (double)o2);
+  const double xm = fmin(fmax(xp, lo), hi);
+  const double x[2] = {xm, -xm};
+  bool ok = isfinite(o1) && isfinite(o2) && isfinite(xeq) &&
+            fabsf(o1 + o2) <= __ldg(F.mlp_norm + 2 * mlp::NI + 1) && xp >= lo - m && xp <= hi + m;
+#pragma unroll
+  for (int k = 0; k < 2; k++) ok = ok && pv[k] + x[k] * V0 > 0.0;
+  atomicAdd(F.mlp_count, 1ull);
+  if (!ok) atomicAdd(F.mlp_count + 1, 1ull);
+  for (int k = 0; k < 2; k++) {
+    const int icp = c0 + k;
+    double cpv = pv[k], cpe = pe[k], cpr = pr[k], cpp = pp[k], cpc = pc[k];
+    if (ok) {
+      const double cpm = F.cpm[icp];
+      cpv = pv[k] + x[k] * V0;
+      cpe = pe[k] - DIV(pbar * (x[k] * V0), maxF(cpm, zc));
+      cpr = DIV(cpm, cpv);
+      eos_pc(C, __ldg(F.icpmat + icp), cpr, cpe, cpp, cpc);
+      F.frvol[icp] = DIV(cpv, V1);
+    }
+    F.cpe[icp] = cpe;
+    F.cpvol[icp] = cpv;
+    F.cprho[icp] = cpr;
+    F.cpp[icp] = cpp;
+    F.cpcs2[icp] = cpc;
+  }
+}
+
 // ================================================================ launchers
 
 static constexpr int BS_DT = 128;
@@ -1457,6 +1587,16 @@ void launch_lag_accel(const DevFields& F, const DevCfg& C, cudaStream_t s) {
 }
 void launch_lag_state(const DevFields& F, const DevCfg& C, cudaStream_t s) {
   k_lag_state<BS_EL, false><<<(F.nel + BS_EL - 1) / BS_EL, BS_EL, 0, s>>>(F, C);
+}
+constexpr size_t kClosureSmem = sizeof(mlp::SmemW) + kClosureWarps * sizeof(mlp::SmemS);
+int prepare_mix_closure() {
+  return cudaFuncSetAttribute(k_mix_closure, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)kClosureSmem) == cudaSuccess ? 0 : -1;
+}
+void launch_mix_closure(const DevFields& F, const DevCfg& C, cudaStream_t s) {
+  if (!F.closure || F.nmx < 1) return;
+  const int per = 16 * kClosureWarps;
+  k_mix_closure<<<(F.nmx + per - 1) / per, 32 * kClosureWarps, kClosureSmem, s>>>(F, C);
 }
 // a batch of meshes: k_getdt over each mesh's own blocks, the rest over all
 // elements or nodes, each reading the step header of its mesh

@@ -257,3 +257,92 @@ def ensemble(n=512, seed=20240607, side_min=32, side_max=512):
             meta = {"kind": "sedov", "side": side, "nx": side, "ny": side, "gamma": gamma}
         out.append((deck, meta))
     return out
+
+
+def sod_interface(nx=2000, ny=200, time_end=0.2, amplitude=0.02, periods=8, seed=7,
+                  rho_right=0.125, p_right=0.1, tilt=0.0):
+    """Two-material Sod tube on [0,1]x[0,0.1] with a sinusoidal interface
+    x = 0.5 + amplitude*sin(2 pi periods y / 0.1 + phase) + tilt*(y - 0.05)
+    (phase drawn from ``seed``): material 1 (gamma 1.4, rho 1, p 1) left of it, material 2
+    (gamma 1.67, rho_right, p_right) right.  Returns (deck, fraction) where
+    ``fraction(cnx, cny)`` gives each cell's area fraction of material 2
+    (Gauss quadrature), for Problem.from_deck(deck, material_fraction=fraction)."""
+    import math
+    import random
+
+    import numpy as np
+    phase = random.Random(seed).uniform(0.0, 2.0 * math.pi)
+    H = 0.1
+    g2 = 1.67
+    e1 = 2.5
+    e2 = p_right / ((g2 - 1.0) * rho_right)
+    deck = f"""&CONTROL
+ time_start=0.0
+ time_end={time_end!r}
+ dt_initial=1.0e-5
+ dt_max=1.0e-3
+ dt_min=1.0e-10
+ dt_g=1.02
+ cfl_sf=0.5
+ cvisc1=0.5
+ cvisc2=0.75
+/
+&EOS
+ eos_type(1)='ideal gas'
+ eos_param(1,1)=1.4
+ eos_type(2)='ideal gas'
+ eos_param(1,2)={g2!r}
+/
+""" + _mesh(nx, ny, 0.0, 0.0, 1.0, H, ("SLIPY", "SLIPX", "SLIPY", "SLIPX")) + f"""&INDICATORS
+ region_type(1)='background'
+ region_name(1)='tube'
+ material_type(1)='background'
+ material_name(1)='left'
+ material_type(2)='shape'
+ material_name(2)='right'
+ material_value(2)=1
+/
+&INITIAL_CONDITIONS
+ thermodynamic_type(1)='region'
+ thermodynamic_value(1)=1
+ density(1)=1.0
+ energy(1)={e1!r}
+ thermodynamic_type(2)='material'
+ thermodynamic_value(2)=2
+ density(2)={rho_right!r}
+ energy(2)={e2!r}
+/
+&SHAPES
+ shape_type(1)='rectangle'
+ shape_param(1,:)=2.0,2.0,3.0,3.0,1.0
+/
+"""
+
+    def interface(y):
+        return (0.5 + amplitude * np.sin(2.0 * np.pi * periods * y / H + phase) +
+                tilt * (y - 0.5 * H))
+
+    def fraction(cnx, cny):
+        x0, x1 = cnx.min(axis=1), cnx.max(axis=1)
+        y0, y1 = cny.min(axis=1), cny.max(axis=1)
+        reach = abs(amplitude) + 0.5 * H * abs(tilt)
+        vf = np.where(x0 >= 0.5 + reach, 1.0, 0.0)
+        band = (x1 > 0.5 - reach) & (x0 < 0.5 + reach)
+        if np.any(band):
+            gx, gw = np.polynomial.legendre.leggauss(8)
+            nsub = 64
+            bx0, bx1, by0, by1 = x0[band], x1[band], y0[band], y1[band]
+            h = (by1 - by0) / nsub
+            acc = np.zeros(len(bx0))
+            for k in range(nsub):
+                a = by0 + k * h
+                for xi, wi in zip(gx, gw):
+                    y = a + 0.5 * h * (xi + 1.0)
+                    wid = np.clip(bx1 - np.maximum(interface(y), bx0), 0.0, bx1 - bx0)
+                    acc += 0.5 * h * wi * wid
+            f = acc / ((bx1 - bx0) * (by1 - by0))
+            f = np.where(f < 1e-12, 0.0, np.where(f > 1.0 - 1e-12, 1.0, f))
+            vf[band] = f
+        return vf
+
+    return deck, fraction

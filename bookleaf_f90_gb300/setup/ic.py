@@ -253,8 +253,11 @@ def eos(cfg, imat, rho, e):
 
 # ---------------------------------------------------------------- IC driver
 
-def apply(groups, mesh, cfg, nreg, nmat, regions, materials, rmesh, mmesh):
-    """Return the dict of initial fields for the mesh (setup_IC + init)."""
+def apply(groups, mesh, cfg, nreg, nmat, regions, materials, rmesh, mmesh,
+          material_fraction=None):
+    """Return the dict of initial fields for the mesh (setup_IC + init).
+    ``material_fraction`` (see Problem.from_deck) overrides the material
+    shapes with per-cell volume fractions of material 2."""
     forms = read_shapes(groups)
     thermo, kin = read_ic(groups)
     nel, nnd = mesh.nel, mesh.nnd
@@ -270,6 +273,14 @@ def apply(groups, mesh, cfg, nreg, nmat, regions, materials, rmesh, mmesh):
     ielmat = mesh.ielmat.copy() if mmesh else np.zeros(nel, np.int32)
     mix = {}                      # iel (1-based) -> list of (material, fraction)
     _flag(materials, ielmat, ielreg, cnx, cny, forms, mix)
+    if material_fraction is not None:
+        if nmat < 2:
+            raise DeckError("ERROR: a material fraction needs two materials")
+        vf = np.asarray(material_fraction(cnx, cny), dtype=np.float64)
+        mix = {}
+        ielmat = np.where(vf >= 1.0, 2, 1).astype(np.int32)
+        for iel in np.nonzero((vf > 0.0) & (vf < 1.0))[0]:
+            mix[int(iel) + 1] = [(1, 1.0 - float(vf[iel])), (2, float(vf[iel]))]
     if np.any(ielmat == 0):
         raise DeckError("ERROR: material not fully populated")
     # flatten: mixed cells in cell order, their components contiguous

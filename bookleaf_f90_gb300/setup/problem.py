@@ -27,14 +27,22 @@ class Problem:
 
     # ------------------------------------------------------------------
     @classmethod
-    def from_deck(cls, path_or_text, name=""):
+    def from_deck(cls, path_or_text, name="", material_fraction=None):
+        """The problem a control file describes.  ``material_fraction``, if
+        given, replaces the deck's material shapes: a function of the
+        elements' corner coordinates (cnx, cny; arrays of shape (nel, 4))
+        returning, per element, the volume fraction of material 2 (material
+        1 fills the rest; cells strictly between 0 and 1 become mixed cells
+        of the two), as a harness can compute exact sub-cell area fractions
+        of an interface that the reference's shapes cannot describe."""
         groups = deckmod.read_deck(path_or_text)
         nreg, nmat, regions, materials, rmesh, mmesh = icmod.read_indicators(groups)
         cfg = deckmod.build_config(groups, nreg, nmat)
         ndx, ndy, indtype, ielnd, ielreg_m, ielmat_m = meshmod.generate(
             groups.get("mesh"), cfg.zerocut)
         mesh = meshmod.Mesh(ndx, ndy, indtype, ielnd, ielreg_m, ielmat_m)
-        st = icmod.apply(groups, mesh, cfg, nreg, nmat, regions, materials, rmesh, mmesh)
+        st = icmod.apply(groups, mesh, cfg, nreg, nmat, regions, materials, rmesh, mmesh,
+                         material_fraction=material_fraction)
         nel, nnd, ncp, nmx = mesh.nel, mesh.nnd, st["ncp"], st["nmx"]
         s = abi.Sizes()
         s.nel = s.nel1 = s.nel2 = nel

@@ -126,6 +126,26 @@ class Solver:
                                            ct.byref(self.error))
         return ierr, list(ms)
 
+    # ---- the learned mixed-cell closure -------------------------------------
+    def set_closure(self, net, norm, on=True):
+        """Let the network net (closure.ClosureNet) split each two-material
+        cell's volume change between its materials from the next Lagrangian
+        step on, with the feature standardisation norm (22 floats, see
+        closure.fit_norm); on=False restores the plain closure."""
+        self._closure = (net, np.ascontiguousarray(norm, dtype=np.float32)) if on else None
+        nm = self._closure[1].ctypes.data_as(ct.c_void_p) if on else None
+        if self.L.bl_set_closure(self.ctx, net.handle if on else None, nm, int(bool(on)),
+                                 ct.byref(self.error)) != 0:
+            raise SolverError(-1, self.error.iout, self.error.message)
+
+    def closure_stats(self):
+        """(mixed-cell steps the closure saw, those it left to the plain
+        closure)."""
+        a, b = ct.c_ulonglong(0), ct.c_ulonglong(0)
+        if self.L.bl_closure_stats(self.ctx, ct.byref(a), ct.byref(b)) != 0:
+            raise RuntimeError("bl_closure_stats failed")
+        return a.value, b.value
+
     @property
     def kernel_launches(self):
         return self.L.bl_kernel_launches(self.ctx)

@@ -260,6 +260,27 @@ int bl_mlp_gradient(bl_mlp *m, const float *x, const float *t, int n, float *gra
 int bl_mlp_train(bl_mlp *m, const float *x, const float *t, int n, int epochs, int batch,
                  float lr, unsigned long long seed, float *losses);
 
+/* The learned mixed-cell closure in a context's Lagrangian step (no
+ * counterpart in the reference, whose closure keeps each material's volume
+ * fraction through the step).  With on = 1, the network net (which must
+ * outlive its use) predicts, for every two-material mixed cell, the volume
+ * each material gains over the step beyond its volume-fraction share, as a
+ * fraction of the cell's volume, norm[20] * output, from ten features of
+ * the cell at the start of the step standardised as (f - norm[k]) *
+ * norm[10 + k]: material 1's volume fraction, the two densities, pressures
+ * and sound speeds squared, dV / V, dt sqrt(max cs2 / V) and (p1 - p2) /
+ * (|p1| + |p2|).  The exchange is limited to the range that moves the two
+ * materials towards pressure equilibrium and not past it.  A cell whose
+ * outputs are not finite, do not cancel within norm[21] (volume
+ * conservation), lie farther outside that range than its width, or leave a
+ * material a non-positive volume keeps the plain closure.  The exchanged
+ * volume trades energy at the mixture pressure, so each cell's volume and
+ * total energy, and every element and node field, are the plain closure's.
+ * on = 0 restores the plain closure everywhere.  Not for batch contexts. */
+int bl_set_closure(bl_ctx *ctx, bl_mlp *net, const float *norm, int on, bl_error *err);
+/* cells the closure has seen and cells it handed back to the plain closure */
+int bl_closure_stats(bl_ctx *ctx, unsigned long long *cells, unsigned long long *rejected);
+
 /* ---- introspection ------------------------------------------------------- */
 
 /* Waits for the context's stream.  Returns 0 or a CUDA error number. */

@@ -1,0 +1,80 @@
+"""Host side of the learned closure (bookleaf_f90_gb300/closure.py): the
+sub-cell aggregation, the features and the standardisation the device
+kernel reads.  No GPU."""
+import numpy as np
+
+from bookleaf_f90_gb300 import Problem, abi, closure, configs
+
+
+def _problem(nx, ny):
+    deck, frac = configs.sod_interface(nx, ny, time_end=0.01)
+    return Problem.from_deck(deck, material_fraction=frac)
+
+
+def test_parameter_layout():
+    p = closure.init_params(3)
+    assert p.dtype == np.float32 and p.size == closure.NPARAM == abi_nparam()
+    # biases start at zero: b1 after W1, b2 after W2, b3 last
+    nh, ni, no = closure.NH, closure.NI, closure.NO
+    assert not np.any(p[nh * ni:nh * ni + nh])
+    assert not np.any(p[-no:])
+
+
+def abi_nparam():
+    import os
+    import re
+    hdr = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                       "bookleaf_gb300.h")
+    return int(re.search(r"#define BL_MLP_NPARAM (\d+)", open(hdr).read()).group(1))
+
+
+def test_fine_material_sums_add_up_to_the_coarse_cells():
+    """Aggregating a 4x-refined mesh over the coarse grid gives each coarse
+    cell the material volumes and masses the coarse mesh itself holds (to
+    the accuracy of the area fractions' quadrature, whose integrand has
+    kinks where the interface leaves a cell)."""
+    nx, ny = 40, 4
+    pc, pf = _problem(nx, ny), _problem(4 * nx, 4 * ny)
+    Vc, Mc, Ec = closure.material_sums(pc, closure.grid_index(pc, nx, ny), nx * ny)
+    Vf, Mf, Ef = closure.material_sums(pf, closure.grid_index(pf, nx, ny), nx * ny)
+    vol = 1.0 / nx * 0.1 / ny
+    assert np.allclose(Vf, Vc, rtol=0, atol=1e-5 * vol)
+    assert np.allclose(Mf, Mc, rtol=0, atol=1e-5 * vol)
+    assert np.allclose(Ef, Ec, rtol=0, atol=3e-5 * vol)
+    assert abs(Vc[:, 1].sum() - 0.05) < 1e-12 and abs(Vc.sum() - 0.1) < 1e-12
+    assert pc.sizes.nmx == int(np.sum((Vc[:, 0] > 0) & (Vc[:, 1] > 0)))
+
+
+def test_features_of_the_initial_interface_cells():
+    nx, ny = 40, 4
+    p = _problem(nx, ny)
+    V, M, E = closure.material_sums(p, closure.grid_index(p, nx, ny), nx * ny)
+    mixed = (V[:, 0] > 0) & (V[:, 1] > 0)
+    X = closure.features(p.config, V[mixed], M[mixed], E[mixed], np.zeros(mixed.sum()), 1e-3)
+    assert X.shape == (mixed.sum(), closure.NI)
+    g2 = 1.67
+    assert np.allclose(X[:, 1], 1.0) and np.allclose(X[:, 2], 0.125)
+    assert np.allclose(X[:, 3], 1.0) and np.allclose(X[:, 4], 0.1)
+    assert np.allclose(X[:, 5], 1.4) and np.allclose(X[:, 6], g2 * 0.1 / 0.125)
+    assert np.allclose(X[:, 0], V[mixed, 0] / V[mixed].sum(axis=1))
+    cell = V[mixed].sum(axis=1)
+    assert np.allclose(X[:, 8], 1e-3 * np.sqrt(1.4 / cell))     # max(1.4, 1.336)
+    assert np.allclose(X[:, 9], 0.9 / 1.1)
+
+
+def test_standardisation_and_exchange():
+    rng = np.random.default_rng(0)
+    X = rng.normal([0.5, 2, 3, 4, 5, 6, 7, 0, 9, 10], [0.1, 2, 3, 4, 5, 6, 7, 1e-3, 9, 0],
+                   (500, 10))
+    x1 = rng.normal(0, 2e-4, 500)
+    fr = np.stack([X[:, 0], 1.0 - X[:, 0]], axis=1)
+    D = fr * X[:, 7:8] + np.stack([x1, -x1], axis=1)      # plain share + exchange
+    norm = closure.fit_norm(X, D)
+    assert norm.shape == (2 * closure.NI + 2,) and norm.dtype == np.float32
+    assert np.allclose(closure.exchange(X, D), np.stack([x1, -x1], axis=1), atol=1e-15)
+    assert abs(norm[20] - np.sqrt(np.mean(x1 ** 2))) < 1e-6 * norm[20]
+    x, t = closure.standardise(X, D, norm)
+    assert np.allclose(x[:, :9].mean(axis=0), 0, atol=1e-5)
+    assert np.allclose(x[:, :9].std(axis=0), 1, atol=1e-4)
+    assert np.all(x[:, 9] == 0) and norm[19] == 1.0       # a constant feature
+    assert np.allclose(t * norm[20], np.stack([x1, -x1], axis=1), rtol=1e-5, atol=1e-12)

@@ -1,0 +1,156 @@
+"""The learned mixed-cell closure on the device (k_mix_closure after
+k_lag_state; bookleaf_f90_gb300/closure.py for the data and training).
+
+- A network whose every prediction fails the checks leaves the run exactly
+  the plain closure's run, bit for bit (exact mode), and the closure counts
+  every two-material cell of every step as handed back.
+- A network trained on the GPU on sub-cell data (4x-refined plain runs of
+  eight interfaces) changes no element or node field of a step and keeps
+  each mixed cell's volume and energy, and on an interface it was not
+  trained on brings the coarse run's material volume fractions and
+  densities closer to the refined run's than the plain closure does."""
+import functools
+
+import numpy as np
+import pytest
+
+from bookleaf_f90_gb300 import Problem, Solver, abi, closure, configs
+from helpers import compare
+
+pytestmark = pytest.mark.gpu
+
+NX, NY, TEND = 160, 16, 0.2
+
+
+# Two-material Sod tubes (pressure and density ratio 1 / s across a planar
+# interface tilted by t): training cases and the held-out one.  Mixed cells
+# get neither artificial viscosity nor hourglass control in the reference's
+# step, so the plain closure only survives mild interfaces like these.
+TRAIN = [(t, s) for t in (0.1, 0.3, 0.4) for s in (0.5, 0.6)] + [(0.1, 0.4), (0.3, 0.4)]
+TEST = (0.2, 0.5)
+
+
+def _make(case, nx, ny):
+    tilt, s = case
+    return configs.sod_interface(nx, ny, time_end=TEND, amplitude=0.0, periods=0, tilt=tilt,
+                                 rho_right=s, p_right=s)
+
+
+def _problem(case, nx=NX, ny=NY):
+    deck, frac = _make(case, nx, ny)
+    return Problem.from_deck(deck, material_fraction=frac)
+
+
+def _run(p, fp, net=None, norm=None):
+    s = Solver(p, fp_mode=fp)
+    if net is not None:
+        s.set_closure(net, norm)
+    ierr, _ = s.run(history=False)
+    assert ierr == 0, s.error.message
+    s.sync_to_host(0)
+    stats = s.closure_stats()
+    launches = s.kernel_launches
+    s.close()
+    return stats, launches
+
+
+def test_rejected_predictions_leave_the_plain_closure_bit_for_bit():
+    # zero weights, b3 = (1000, 1000): both outputs predict a volume change
+    # far from the cell's, which the conservation check rejects everywhere
+    params = np.zeros(closure.NPARAM, np.float32)
+    params[-2:] = 1000.0
+    net = closure.ClosureNet(params)
+    norm = np.concatenate([np.zeros(closure.NI), np.ones(closure.NI), [1e-3, 0.1]])
+    pa, pb = _problem(TEST, 80, 8), _problem(TEST, 80, 8)
+    sa, la = _run(pa, abi.FP_EXACT)
+    sb, lb = _run(pb, abi.FP_EXACT, net, norm)
+    assert sa == (0, 0)
+    nstep = pb.timestep.nstep
+    assert nstep == pa.timestep.nstep > 50
+    assert sb == (pb.sizes.nmx * nstep, pb.sizes.nmx * nstep)
+    assert lb - la == nstep        # one closure kernel per step
+    assert not compare(pa, pb, exact=True)
+    net.close()
+
+
+@pytest.fixture(scope="module")
+def trained():
+    Xs, Ds = [], []
+    for case in TRAIN:
+        X, D, _ = closure.subcell_samples(functools.partial(_make, case), NX, NY)
+        Xs.append(X)
+        Ds.append(D)
+    X, D = np.concatenate(Xs), np.concatenate(Ds)
+    net, norm, losses = closure.train(X, D, epochs=100)
+    yield net, norm, losses, X, D
+    net.close()
+
+
+def test_training_fits_the_subcell_volume_changes(trained):
+    net, norm, losses, X, D = trained
+    assert losses[-1] < 0.1 * losses[0]
+    x, t = closure.standardise(X, D, norm)
+    y = net.predict(x)
+    # the plain closure is a zero exchange
+    assert np.sqrt(np.mean((y - t) ** 2)) < 0.3 * np.sqrt(np.mean(t ** 2))
+    assert np.mean(np.abs(y[:, 0] + y[:, 1]) <= norm[2 * closure.NI + 1]) > 0.9
+
+
+def _cell_sums(p):
+    f, nmx = p.fields, p.sizes.nmx
+    cp_el = np.repeat(f[abi.IMXEL][:nmx] - 1, f[abi.IMXNCP][:nmx])
+    n = len(cp_el)
+    out = []
+    for w in (f[abi.CPVOLUME][:n], f[abi.CPMASS][:n] * f[abi.CPENERGY][:n], f[abi.FRVOLUME][:n]):
+        acc = np.zeros(p.sizes.nel)
+        np.add.at(acc, cp_el, w)
+        out.append(acc[f[abi.IMXEL][:nmx] - 1])
+    return out
+
+
+def test_one_learned_step_keeps_cell_volumes_energies_and_all_element_fields(trained):
+    """From the same state, one step with the learned closure leaves every
+    element and node field as the plain step does, bit for bit, and in each
+    mixed cell the materials' volumes and internal energies add up to the
+    plain step's (the exchange sums to zero), while the materials' own
+    volumes do change."""
+    net, norm = trained[:2]
+    pp, pl = _problem(TEST), _problem(TEST)
+    sp, sl = Solver(pp, fp_mode=abi.FP_EXACT), Solver(pl, fp_mode=abi.FP_EXACT)
+    for s in (sp, sl):
+        ierr, _ = s.run(max_steps=40, history=False)
+        assert ierr == 0
+    sl.set_closure(net, norm)
+    assert sp.step() == 0 and sl.step() == 0
+    cells, rejected = sl.closure_stats()
+    assert cells == pl.sizes.nmx and rejected < 0.5 * cells
+    for s in (sp, sl):
+        s.sync_to_host(0)
+        s.close()
+    for fid in (abi.ELDENSITY, abi.ELENERGY, abi.ELPRESSURE, abi.ELVOLUME, abi.NDX, abi.NDY,
+                abi.NDU, abi.NDV, abi.ELMASS, abi.CPMASS):
+        assert np.array_equal(pp.fields[fid], pl.fields[fid]), abi.NAMES[fid]
+    (vp, ep, fp), (vl, el, fl) = _cell_sums(pp), _cell_sums(pl)
+    assert np.allclose(vl, vp, rtol=1e-13, atol=0)
+    assert np.allclose(el, ep, rtol=1e-12, atol=0)
+    assert np.allclose(fl, 1.0, rtol=0, atol=1e-13)
+    moved = np.abs(pl.fields[abi.CPVOLUME] - pp.fields[abi.CPVOLUME]) / pp.fields[abi.CPVOLUME]
+    assert np.sum(moved > 1e-9) >= 0.25 * len(moved)   # cells at equilibrium keep x = 0
+
+
+def test_learned_closure_beats_the_plain_closure_on_an_unseen_interface(trained):
+    net, norm = trained[:2]
+    _, _, truth = closure.subcell_samples(functools.partial(_make, TEST), NX, NY, lags=(1,))
+    errs, stats = {}, None
+    for mode in ("plain", "learned"):
+        p = _problem(TEST)
+        idx = closure.grid_index(p, NX, NY)
+        cells = idx[p.fields[abi.IMXEL][:p.sizes.nmx] - 1]
+        st, _ = _run(p, abi.FP_FAST, *((net, norm) if mode == "learned" else ()))
+        if mode == "learned":
+            stats = st
+        errs[mode] = closure.mixed_errors(p, idx, truth, cells)
+    (fp, r1p, r2p), (fl, r1l, r2l) = errs["plain"], errs["learned"]
+    assert stats[1] < 0.3 * stats[0], stats
+    assert fl < 0.5 * fp, errs
+    assert r1l < 0.5 * r1p and r2l < 0.5 * r2p, errs

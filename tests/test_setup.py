@@ -118,3 +118,20 @@ def test_reference_decks_parse():
             continue
         p = Problem.from_deck(text)
         assert p.nel > 0 and np.all(p.fields[abi.ELVOLUME] > 0), os.path.basename(d)
+
+
+def test_sinusoidal_interface_fractions_are_exact_areas():
+    """The two-material Sod's cell fractions of material 2 add up to its
+    area (half the tube: the sine integrates to zero over whole periods),
+    and the mixed cells straddle the interface."""
+    import numpy as np
+    from bookleaf_f90_gb300 import Problem, abi, configs
+    deck, frac = configs.sod_interface(200, 20, time_end=0.01)
+    p = Problem.from_deck(deck, material_fraction=frac)
+    nd = p.fields[abi.IELND].reshape(-1, 4) - 1
+    cnx, cny = p.fields[abi.NDX][nd], p.fields[abi.NDY][nd]
+    vf = frac(cnx, cny)
+    area = p.fields[abi.ELVOLUME]
+    assert abs(np.sum(vf * area) - 0.05) <= 1e-9
+    assert p.sizes.nmx == int(np.sum((vf > 0) & (vf < 1))) > 20
+    assert p.sizes.ncp == 2 * p.sizes.nmx
