@@ -274,3 +274,36 @@ def mixed_errors(problem, index, truth, cells):
     rhot = Mt[cells] / Vt[cells]
     rel = np.abs(rho - rhot) / rhot
     return float(np.mean(np.abs(fr - frt))), float(np.mean(rel[:, 0])), float(np.mean(rel[:, 1]))
+
+
+def interface_positions(problem, index, nx, ny):
+    """Per row of the coarse grid, the position of the interface as the
+    share of the row's volume that is material 1 times the tube's length
+    (material 1 fills the left; exact for an interface across the rows)."""
+    V, _, _ = material_sums(problem, index, nx * ny)
+    x = problem.fields[abi.NDX]
+    row = V.reshape(ny, nx, 2).sum(axis=1)
+    return x.min() + row[:, 0] / row.sum(axis=1) * (x.max() - x.min())
+
+
+def against_plain(learned, plain, index, nx, ny):
+    """The learned closure's run against the plain closure's on the same
+    mesh: (largest shift of the interface in any row, in cells; relative L1
+    difference of the mixed cells' densities; of all cells' densities)."""
+    dx = (plain.fields[abi.NDX].max() - plain.fields[abi.NDX].min()) / nx
+    shift = np.max(np.abs(interface_positions(learned, index, nx, ny) -
+                          interface_positions(plain, index, nx, ny))) / dx
+    el = plain.fields[abi.IMXEL][:plain.sizes.nmx] - 1
+    rl, rp = learned.fields[abi.ELDENSITY], plain.fields[abi.ELDENSITY]
+    return (float(shift), float(np.sum(np.abs(rl[el] - rp[el])) / np.sum(np.abs(rp[el]))),
+            float(np.sum(np.abs(rl - rp)) / np.sum(np.abs(rp))))
+
+
+def cell_density_error(problem, index, truth, cells):
+    """Relative L1 error of the given cells' densities (the cell's mass over
+    its volume) against the sub-cell truth (V, M)."""
+    el = problem.fields[abi.IMXEL][:problem.sizes.nmx] - 1
+    Vt, Mt = truth
+    rt = Mt[cells].sum(axis=1) / Vt[cells].sum(axis=1)
+    r = problem.fields[abi.ELDENSITY][el]
+    return float(np.sum(np.abs(r - rt)) / np.sum(rt))
