@@ -18,6 +18,7 @@
 #include "bl_device.cuh"
 #include "bl_ctx.h"
 #include "bl_kernels.h"
+#include "bl_mma.cuh"
 
 using bl::DevStep;
 using bl::d4;
@@ -1485,7 +1486,7 @@ int bl_run_batch(bl_ctx* x, bl_timestep* ts, int max_steps, int* status, int* ns
 
 int bl_batch_size(bl_ctx* x) { return x ? x->ninst : 0; }
 
-const float* bl_mlp_device_params(bl_mlp* m);  // bl_mlp.cu
+const float* bl_mlp_device_image(bl_mlp* m);  // bl_mlp.cu
 
 int bl_set_closure(bl_ctx* x, bl_mlp* net, const float* norm, int on, bl_error* e) {
   set_err(e, BL_SUCCESS, BL_HALT_SINGLE, "");
@@ -1499,10 +1500,14 @@ int bl_set_closure(bl_ctx* x, bl_mlp* net, const float* norm, int on, bl_error* 
     if (!F.mxv0) F.mxv0 = dalloc<double>(x, std::max(1, x->s.nmx), st);
     if (!F.mlp_norm) F.mlp_norm = dalloc<float>(x, 2 * BL_MLP_IN + 2, st);
     if (!F.mlp_count) F.mlp_count = dalloc<unsigned long long>(x, 2, st);
+    if (!F.mlp_img) F.mlp_img = dalloc<float>(x, bl::mlp::kImgN, st);
     if (st != cudaSuccess || x->L.mix_prepare() != 0) return cuda_fail(e, cudaErrorMemoryAllocation, "bl_set_closure");
     cudaMemcpyAsync(const_cast<float*>(F.mlp_norm), norm, (2 * BL_MLP_IN + 2) * sizeof(float),
                     cudaMemcpyHostToDevice, x->stream);
-    F.mlp_params = bl_mlp_device_params(net);
+    // the network as it is now (training it further changes nothing here)
+    cudaDeviceSynchronize();
+    cudaMemcpyAsync(F.mlp_img, bl_mlp_device_image(net), bl::mlp::kImgN * sizeof(float),
+                    cudaMemcpyDeviceToDevice, x->stream);
   }
   F.closure = on ? 1 : 0;
   // the device loop's graph holds the old arguments

@@ -131,8 +131,10 @@ struct DevFields {
   int nd_block;              // block size of the batch's node kernels (autotuned)
   // learned mixed-cell closure (bl_set_closure; off when closure == 0)
   int closure;
-  const float* mlp_params;   // the network's FP32 parameters (bl_mlp.cu layout)
-  const float* mlp_norm;     // [20]: feature means, then inverse spreads
+  float* mlp_img;            // the network's parameters as their shared-memory
+                             // image (bl_mma.cuh), copied at bl_set_closure
+  const float* mlp_norm;     // [22]: feature means, inverse spreads, output
+                             // scale, conservation tolerance
   double* mxv0;              // [nmx] cell volume at the start of the step
   unsigned long long* mlp_count;  // [2]: cells the closure saw, cells it rejected
 };

@@ -35,12 +35,12 @@ __device__ void load_x(SmemS& s, const float* X, int base, int n) {
   __syncwarp();
 }
 
-__global__ void __launch_bounds__(TPB) k_mlp_forward(const float* P, const float* X, float* Y,
+__global__ void __launch_bounds__(TPB) k_mlp_forward(const float* img, const float* X, float* Y,
                                                      int n) {
   extern __shared__ unsigned char smem[];
   SmemW& w = *reinterpret_cast<SmemW*>(smem);
   SmemS* S = reinterpret_cast<SmemS*>(smem + sizeof(SmemW));
-  load_weights(w, P);
+  copy_weights<TPB>(w, img);
   __syncthreads();
   const int warp = threadIdx.x >> 5;
   SmemS& s = S[warp];
@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(TPB) k_mlp_forward(const float* P, const float
 
 // Forward and backward of one block's 64 samples; the block's gradient sum
 // and loss sum go to G[blockIdx][NP] and L[blockIdx].
-__global__ void __launch_bounds__(TPB) k_mlp_grad(const float* P, const float* X, const float* T,
+__global__ void __launch_bounds__(TPB) k_mlp_grad(const float* img, const float* X, const float* T,
                                                   const int* idx, int n, float inv_n, float* G,
                                                   float* L) {
   extern __shared__ unsigned char smem[];
@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(TPB) k_mlp_grad(const float* P, const float* X
   float(*dz2)[NH] = dz1 + SPB;
   float(*dy)[16] = reinterpret_cast<float(*)[16]>(dz2 + SPB);
   float* lsum = reinterpret_cast<float*>(dy + SPB);
-  load_weights(w, P);
+  copy_weights<TPB>(w, img);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x < WARPS) lsum[threadIdx.x] = 0.0f;
   __syncthreads();
@@ -190,8 +190,10 @@ __global__ void __launch_bounds__(TPB) k_mlp_grad(const float* P, const float* X
   if (threadIdx.x == 0) L[blockIdx.x] = 0.5f * inv_n * (lsum[0] + lsum[1] + lsum[2] + lsum[3]);
 }
 
-// Sums the per-block gradients and losses in block order.
-__global__ void k_mlp_reduce(const float* G, const float* L, int nblk, float* grad, float* loss) {
+// Sums the per-block gradients and losses in block order; the loss times
+// wgt is also added to *acc (an epoch's running sum), in launch order.
+__global__ void k_mlp_reduce(const float* G, const float* L, int nblk, float* grad, float* loss,
+                             double* acc, double wgt) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < NP) {
     float s = 0.0f;
@@ -202,19 +204,29 @@ __global__ void k_mlp_reduce(const float* G, const float* L, int nblk, float* gr
     float s = 0.0f;
     for (int b = 0; b < nblk; b++) s += L[b];
     *loss = s;
+    if (acc) *acc += (double)s * wgt;
   }
 }
 
+// The parameters' shared-memory image (its padding is zeroed once).
+__global__ void k_mlp_image(const float* P, float* img) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < NP) img[image_offset(i)] = P[i];
+}
+
 // Adam on the FP32 master parameters (Kingma and Ba, 2015).
-__global__ void k_mlp_adam(float* P, float* M, float* V, const float* grad, float lr, float b1,
-                           float b2, float eps, float c1, float c2) {
+// The image is kept current with the parameters.
+__global__ void k_mlp_adam(float* P, float* M, float* V, float* img, const float* grad, float lr,
+                           float b1, float b2, float eps, float c1, float c2) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= NP) return;
   const float g = grad[i];
   const float m = b1 * M[i] + (1.0f - b1) * g, v = b2 * V[i] + (1.0f - b2) * g * g;
   M[i] = m;
   V[i] = v;
-  P[i] -= lr * (m * c1) / (sqrtf(v * c2) + eps);
+  const float p = P[i] - lr * (m * c1) / (sqrtf(v * c2) + eps);
+  P[i] = p;
+  img[image_offset(i)] = p;
 }
 
 constexpr size_t kSmemFwd = sizeof(SmemW) + WARPS * sizeof(SmemS);
@@ -224,6 +236,8 @@ constexpr size_t kSmemGrad = kSmemFwd + (2 * SPB * NH + SPB * 16 + WARPS) * size
 
 struct bl_mlp {
   float *P = nullptr, *M = nullptr, *V = nullptr, *grad = nullptr, *loss = nullptr;
+  float* img = nullptr;  // SmemW image of P
+  double* acc = nullptr;  // an epoch's loss sum
   int step = 0;
 };
 
@@ -237,10 +251,17 @@ int bl_mlp_create(bl_mlp** out, const float* params) {
             cudaMalloc(&m->M, NP * sizeof(float)) == cudaSuccess &&
             cudaMalloc(&m->V, NP * sizeof(float)) == cudaSuccess &&
             cudaMalloc(&m->grad, NP * sizeof(float)) == cudaSuccess &&
-            cudaMalloc(&m->loss, sizeof(float)) == cudaSuccess;
+            cudaMalloc(&m->loss, sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&m->img, kImgN * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&m->acc, sizeof(double)) == cudaSuccess;
   ok = ok && cudaMemcpy(m->P, params, NP * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess &&
        cudaMemset(m->M, 0, NP * sizeof(float)) == cudaSuccess &&
-       cudaMemset(m->V, 0, NP * sizeof(float)) == cudaSuccess;
+       cudaMemset(m->V, 0, NP * sizeof(float)) == cudaSuccess &&
+       cudaMemset(m->img, 0, kImgN * sizeof(float)) == cudaSuccess;
+  if (ok) {
+    k_mlp_image<<<(NP + 255) / 256, 256>>>(m->P, m->img);
+    ok = cudaDeviceSynchronize() == cudaSuccess;
+  }
   ok = ok && cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kSmemFwd) == cudaSuccess &&
        cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -260,6 +281,8 @@ int bl_mlp_destroy(bl_mlp* m) {
   cudaFree(m->V);
   cudaFree(m->grad);
   cudaFree(m->loss);
+  cudaFree(m->img);
+  cudaFree(m->acc);
   delete m;
   return BL_SUCCESS;
 }
@@ -270,7 +293,9 @@ int bl_mlp_params(bl_mlp* m, float* params) {
              ? BL_SUCCESS : BL_FAILURE;
 }
 
-const float* bl_mlp_device_params(bl_mlp* m) { return m ? m->P : nullptr; }
+// The device image of the current parameters (the layout the closure
+// kernel copies into shared memory); bl_set_closure takes a copy.
+const float* bl_mlp_device_image(bl_mlp* m) { return m ? m->img : nullptr; }
 
 int bl_mlp_predict(bl_mlp* m, const float* x, int n, float* y) {
   if (!m || !x || !y || n < 0) return BL_FAILURE;
@@ -280,7 +305,7 @@ int bl_mlp_predict(bl_mlp* m, const float* x, int n, float* y) {
             cudaMalloc(&dy, (size_t)n * NO * sizeof(float)) == cudaSuccess;
   ok = ok && cudaMemcpy(dx, x, (size_t)n * NI * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
   if (ok) {
-    k_mlp_forward<<<(n + SPB - 1) / SPB, TPB, kSmemFwd>>>(m->P, dx, dy, n);
+    k_mlp_forward<<<(n + SPB - 1) / SPB, TPB, kSmemFwd>>>(m->img, dx, dy, n);
     ok = cudaMemcpy(y, dy, (size_t)n * NO * sizeof(float), cudaMemcpyDeviceToHost) == cudaSuccess;
   }
   cudaFree(dx);
@@ -299,8 +324,8 @@ int bl_mlp_gradient(bl_mlp* m, const float* x, const float* t, int n, float* gra
   ok = ok && cudaMemcpy(dx, x, (size_t)n * NI * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess &&
        cudaMemcpy(dt, t, (size_t)n * NO * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
   if (ok) {
-    k_mlp_grad<<<nblk, TPB, kSmemGrad>>>(m->P, dx, dt, nullptr, n, 1.0f / (float)n, G, L);
-    k_mlp_reduce<<<(NP + 255) / 256, 256>>>(G, L, nblk, m->grad, m->loss);
+    k_mlp_grad<<<nblk, TPB, kSmemGrad>>>(m->img, dx, dt, nullptr, n, 1.0f / (float)n, G, L);
+    k_mlp_reduce<<<(NP + 255) / 256, 256>>>(G, L, nblk, m->grad, m->loss, nullptr, 0.0);
     ok = cudaMemcpy(grad, m->grad, NP * sizeof(float), cudaMemcpyDeviceToHost) == cudaSuccess;
     if (ok && loss) ok = cudaMemcpy(loss, m->loss, sizeof(float), cudaMemcpyDeviceToHost) == cudaSuccess;
   }
@@ -339,21 +364,24 @@ int bl_mlp_train(bl_mlp* m, const float* x, const float* t, int n, int epochs, i
       const int j = (int)(z % (uint64_t)(i + 1));
       std::swap(perm[i], perm[j]);
     }
-    ok = cudaMemcpy(didx, perm.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess;
-    double eloss = 0.0;
+    ok = cudaMemcpy(didx, perm.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemset(m->acc, 0, sizeof(double)) == cudaSuccess;
+    // the epoch's mini-batches queue without host round trips; its loss is
+    // summed on the device and read once
     for (int b0 = 0; b0 < n && ok; b0 += batch) {
       const int nb = std::min(batch, n - b0);
       const int nblk = (nb + SPB - 1) / SPB;
-      k_mlp_grad<<<nblk, TPB, kSmemGrad>>>(m->P, dx, dt, didx + b0, nb, 1.0f / (float)nb, G, L);
-      k_mlp_reduce<<<(NP + 255) / 256, 256>>>(G, L, nblk, m->grad, m->loss);
+      k_mlp_grad<<<nblk, TPB, kSmemGrad>>>(m->img, dx, dt, didx + b0, nb, 1.0f / (float)nb, G, L);
+      k_mlp_reduce<<<(NP + 255) / 256, 256>>>(G, L, nblk, m->grad, m->loss, m->acc, (double)nb);
       m->step++;
       const float c1 = 1.0f / (1.0f - powf(b1, (float)m->step));
       const float c2 = 1.0f / (1.0f - powf(b2, (float)m->step));
-      k_mlp_adam<<<(NP + 255) / 256, 256>>>(m->P, m->M, m->V, m->grad, lr, b1, b2, eps, c1, c2);
-      float lb = 0.0f;
-      ok = cudaMemcpy(&lb, m->loss, sizeof(float), cudaMemcpyDeviceToHost) == cudaSuccess;
-      eloss += (double)lb * nb;
+      k_mlp_adam<<<(NP + 255) / 256, 256>>>(m->P, m->M, m->V, m->img, m->grad, lr, b1, b2, eps,
+                                            c1, c2);
     }
+    double eloss = 0.0;
+    ok = ok && cudaGetLastError() == cudaSuccess &&
+         cudaMemcpy(&eloss, m->acc, sizeof(double), cudaMemcpyDeviceToHost) == cudaSuccess;
     if (losses) losses[ep] = (float)(eloss / n);
   }
   ok = ok && cudaDeviceSynchronize() == cudaSuccess;

@@ -77,21 +77,37 @@ __device__ __forceinline__ float sigm(float z) { return 1.0f / (1.0f + __expf(-z
 struct SmemW {
   float w1[NH][16], b1[NH], w2[NH][NH], b2[NH], w3[16][NH], b3[16];
 };
-static __device__ void load_weights(SmemW& w, const float* P) {
-  for (int i = threadIdx.x; i < NH * 16; i += blockDim.x) {
-    const int r = i / 16, c = i % 16;
-    w.w1[r][c] = c < NI ? P[OW1 + r * NI + c] : 0.0f;
+// The image of SmemW in global memory: the offset of parameter i in it
+// (the padding stays zero).  Kernels copy the image with 16-byte loads, all
+// issued before the first store, instead of gathering and padding the
+// parameters one by one.
+constexpr int kImgB1 = NH * 16, kImgW2 = kImgB1 + NH, kImgB2 = kImgW2 + NH * NH,
+              kImgW3 = kImgB2 + NH, kImgB3 = kImgW3 + 16 * NH, kImgN = kImgB3 + 16;
+static_assert(kImgN * sizeof(float) == sizeof(SmemW) && sizeof(SmemW) % 16 == 0, "image");
+__host__ __device__ constexpr int image_offset(int i) {
+  return i < OB1   ? (i / NI) * 16 + i % NI
+         : i < OW2 ? kImgB1 + (i - OB1)
+         : i < OB2 ? kImgW2 + (i - OW2)
+         : i < OW3 ? kImgB2 + (i - OB2)
+         : i < OB3 ? kImgW3 + (i - OW3)
+                   : kImgB3 + (i - OB3);
+}
+template <int NT>
+__device__ __forceinline__ void copy_weights(SmemW& w, const float* img) {
+  constexpr int N4 = kImgN / 4, K = (N4 + NT - 1) / NT;
+  const float4* src = reinterpret_cast<const float4*>(img);
+  float4* dst = reinterpret_cast<float4*>(&w);
+  float4 r[K];
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    const int i = threadIdx.x + k * NT;
+    if (i < N4) r[k] = __ldg(src + i);
   }
-  for (int i = threadIdx.x; i < NH * NH; i += blockDim.x) w.w2[i / NH][i % NH] = P[OW2 + i];
-  for (int i = threadIdx.x; i < 16 * NH; i += blockDim.x) {
-    const int r = i / NH, c = i % NH;
-    w.w3[r][c] = r < NO ? P[OW3 + r * NH + c] : 0.0f;
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    const int i = threadIdx.x + k * NT;
+    if (i < N4) dst[i] = r[k];
   }
-  for (int i = threadIdx.x; i < NH; i += blockDim.x) {
-    w.b1[i] = P[OB1 + i];
-    w.b2[i] = P[OB2 + i];
-  }
-  for (int i = threadIdx.x; i < 16; i += blockDim.x) w.b3[i] = i < NO ? P[OB3 + i] : 0.0f;
 }
 
 // One warp's 16 samples: x (16x16, padded), pre-activations and activations

@@ -1472,7 +1472,7 @@ __global__ void __launch_bounds__(32 * kClosureWarps) k_mix_closure(DevFields F,
   extern __shared__ unsigned char smem[];
   mlp::SmemW& w = *reinterpret_cast<mlp::SmemW*>(smem);
   mlp::SmemS* Ss = reinterpret_cast<mlp::SmemS*>(smem + sizeof(mlp::SmemW));
-  mlp::load_weights(w, F.mlp_params);
+  mlp::copy_weights<32 * kClosureWarps>(w, F.mlp_img);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   mlp::SmemS& s = Ss[warp];

@@ -128,12 +128,15 @@ class Solver:
 
     # ---- the learned mixed-cell closure -------------------------------------
     def set_closure(self, net, norm, on=True):
-        """Let the network net (closure.ClosureNet) split each two-material
-        cell's volume change between its materials from the next Lagrangian
-        step on, with the feature standardisation norm (22 floats, see
-        closure.fit_norm); on=False restores the plain closure."""
-        self._closure = (net, np.ascontiguousarray(norm, dtype=np.float32)) if on else None
-        nm = self._closure[1].ctypes.data_as(ct.c_void_p) if on else None
+        """Let the network net (closure.ClosureNet; its current parameters
+        are copied) split each two-material cell's volume change between its
+        materials from the next Lagrangian step on, with the feature
+        standardisation norm (22 floats, see closure.fit_norm); on=False
+        restores the plain closure."""
+        nm_arr = np.ascontiguousarray(norm, dtype=np.float32) if on else None
+        if on and nm_arr.size != 22:
+            raise ValueError("norm needs 22 floats")
+        nm = nm_arr.ctypes.data_as(ct.c_void_p) if on else None
         if self.L.bl_set_closure(self.ctx, net.handle if on else None, nm, int(bool(on)),
                                  ct.byref(self.error)) != 0:
             raise SolverError(-1, self.error.iout, self.error.message)

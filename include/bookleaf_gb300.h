@@ -262,8 +262,9 @@ int bl_mlp_train(bl_mlp *m, const float *x, const float *t, int n, int epochs, i
 
 /* The learned mixed-cell closure in a context's Lagrangian step (no
  * counterpart in the reference, whose closure keeps each material's volume
- * fraction through the step).  With on = 1, the network net (which must
- * outlive its use) predicts, for every two-material mixed cell, the volume
+ * fraction through the step).  With on = 1, the network net (its current
+ * parameters are copied: it may be trained further or destroyed after the
+ * call) predicts, for every two-material mixed cell, the volume
  * each material gains over the step beyond its volume-fraction share, as a
  * fraction of the cell's volume, norm[20] * output, from ten features of
  * the cell at the start of the step standardised as (f - norm[k]) *
