@@ -375,10 +375,24 @@ def run_closure(args, torch):
     deck, frac = _closure_case(CLOSURE_TEST, nx, ny)
     pp = Problem.from_deck(deck, material_fraction=frac)
     pl = pp.copy()
+    pe = pp.copy()
     idx = closure.grid_index(pp, nx, ny)
     cells = idx[pp.fields[abi.IMXEL][:pp.sizes.nmx] - 1]
     rp = timed(pp, False, 20000)
     rl = timed(pl, True, 20000)
+    # e2e: the host arrays registered (bl_init uploads them), the closure
+    # set, the run through the device loop, the whole state downloaded
+    h2d = sum(a.nbytes for a in pe.fields.values())
+    torch.cuda.synchronize()
+    t4 = time.perf_counter()
+    se = Solver(pe, fp_mode=fp)
+    se.set_closure(net, norm)
+    ierr_e, _ = se.run(max_steps=20000, history=False)
+    se.sync_to_host(0)
+    t5 = time.perf_counter()
+    assert ierr_e == 0, se.error.message
+    ne = pe.timestep.nstep
+    se.close()
     # the same interface 4x refined, plain: the sub-cell truth at the end
     t3 = time.perf_counter()
     deck4, frac4 = _closure_case(CLOSURE_TEST, 4 * nx, 4 * ny)
@@ -441,6 +455,11 @@ def run_closure(args, torch):
                          "peak_kind": peak_kind,
                          "note": "algorithmic bytes 724 B per zone-cycle (Lagrangian); the "
                                  "FP64 issue rate, not HBM, bounds the path"},
+            "e2e": {"value": pe.nel * ne / (t5 - t4), "unit": "zone-cycles/s",
+                    "h2d_bytes_per_step": int(h2d / max(1, ne)),
+                    "d2h_bytes_per_step": int(h2d / max(1, ne)),
+                    "note": "bl_init from the host arrays + bl_set_closure + %d steps of the "
+                            "device loop + full download, wall clock" % ne},
             "gpu_launches": rl["launches"], "clocks": rl["clocks"]}
 
 

@@ -307,3 +307,41 @@ def cell_density_error(problem, index, truth, cells):
     rt = Mt[cells].sum(axis=1) / Vt[cells].sum(axis=1)
     r = problem.fields[abi.ELDENSITY][el]
     return float(np.sum(np.abs(r - rt)) / np.sum(rt))
+
+
+def main(argv=None):
+    """A small end-to-end run: sub-cell samples of one tilted two-material
+    tube, a short training, then that tube coarse with the learned closure
+    for a number of steps; prints what it did.  Used as the profiling case
+    of the closure's kernels (k_mlp_grad, k_mix_closure)."""
+    import argparse
+    import functools
+    from .setup import Problem, configs
+    from .solver import Solver
+    ap = argparse.ArgumentParser(prog="python -m bookleaf_f90_gb300.closure")
+    ap.add_argument("--nx", type=int, default=160)
+    ap.add_argument("--epochs", type=int, default=2)
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--tilt", type=float, default=0.2)
+    ap.add_argument("--state", type=float, default=0.5)
+    a = ap.parse_args(argv)
+    ny = max(1, a.nx // 10)
+    make = functools.partial(configs.sod_interface, time_end=0.02, amplitude=0.0, periods=0,
+                             tilt=a.tilt, rho_right=a.state, p_right=a.state)
+    X, D, _ = subcell_samples(make, a.nx, ny)
+    net, norm, losses = train(X, D, epochs=a.epochs)
+    deck, fraction = make(a.nx, ny)
+    p = Problem.from_deck(deck, material_fraction=fraction)
+    s = Solver(p)
+    s.set_closure(net, norm)
+    ierr, _ = s.run(max_steps=a.steps, history=False)
+    seen, rejected = s.closure_stats()
+    print("samples %d, loss %.4g -> %.4g, %d steps (ierr %d), closure cells %d, rejected %d"
+          % (len(X), losses[0], losses[-1], p.timestep.nstep, ierr, seen, rejected))
+    s.close()
+    net.close()
+    return ierr
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
