@@ -5,7 +5,8 @@ describes, with its own mesh, materials, time-step controls and end time --
 with bl_init_batch, and advances them with bl_run_batch: one kernel per
 phase over all the meshes, each mesh keeping its own dt and time on the
 device.  Every mesh ends as it would running alone (bit for bit in exact
-mode).  ``sync_to_host`` updates each Problem's own arrays.
+mode), mixed cells and the learned closure included.  ``sync_to_host``
+updates each Problem's own arrays.
 """
 import ctypes as ct
 
@@ -65,6 +66,18 @@ class BatchSolver:
             raise SolverError(ierr, self.error.iout, self.error.message)
         cand = [(G, B) for G in (8, 16, 32) for B in (128, 256, 512)]
         return g.value, bs.value, dict(zip(cand, list(ms)))
+
+    def set_closure(self, net, norm, on=True):
+        """The learned mixed-cell closure for every mesh of the batch (see
+        Solver.set_closure)."""
+        from .solver import Solver
+        Solver.set_closure(self, net, norm, on)
+
+    def closure_stats(self):
+        """(mixed-cell steps the closure saw, those it left to the plain
+        closure), over all meshes."""
+        from .solver import Solver
+        return Solver.closure_stats(self)
 
     def sync_to_host(self, fid=0):
         return self.L.bl_sync_to_host(self.ctx, fid)

@@ -32,14 +32,14 @@ const bl::Launchers kFast = {bl::fast::getdt_blocks,          bl::fast::launch_g
                              bl::fast::launch_getdt_batch,     bl::fast::launch_lag_force_batch,
                              bl::fast::launch_lag_accel_batch, bl::fast::launch_lag_state_batch,
                              bl::fast::launch_ale_batch,       bl::fast::prepare_mix_closure,
-                             bl::fast::launch_mix_closure};
+                             bl::fast::launch_mix_closure,     bl::fast::launch_mix_closure_batch};
 const bl::Launchers kExact = {bl::exact::getdt_blocks,          bl::exact::launch_getdt,
                               bl::exact::launch_lag_force,       bl::exact::launch_lag_accel,
                               bl::exact::launch_lag_state,       bl::exact::launch_ale,
                               bl::exact::launch_getdt_batch,     bl::exact::launch_lag_force_batch,
                               bl::exact::launch_lag_accel_batch, bl::exact::launch_lag_state_batch,
                               bl::exact::launch_ale_batch,       bl::exact::prepare_mix_closure,
-                              bl::exact::launch_mix_closure};
+                              bl::exact::launch_mix_closure,     bl::exact::launch_mix_closure_batch};
 
 // batches (defined with bl_init_batch below)
 void batch_copy(bl_ctx* x, int id, bool to_mesh);
@@ -95,7 +95,8 @@ const int kStateIds[] = {BL_ELDENSITY, BL_ELENERGY, BL_ELPRESSURE, BL_ELCS2, BL_
                          BL_A1, BL_A2, BL_A3, BL_B1, BL_B2, BL_B3, BL_CNWT, BL_CNX, BL_CNY,
                          BL_CNVISCX, BL_CNVISCY, BL_ELVISC, BL_ELMASS, BL_CNMASS, BL_NDX,
                          BL_NDY, BL_NDU, BL_NDV, BL_CPDENSITY, BL_CPENERGY, BL_CPPRESSURE,
-                         BL_CPCS2, BL_CPVOLUME, BL_CPA1, BL_CPA3, BL_CPB1, BL_CPB3};
+                         BL_CPCS2, BL_CPVOLUME, BL_FRVOLUME, BL_CPA1, BL_CPA3, BL_CPB1,
+                         BL_CPB3};
 
 bool ale_active(const bl_config& c, double time) {  // ale_dr_utils.f90:35-51
   if (!c.ale_zexist) return false;
@@ -962,6 +963,7 @@ static size_t field_count(const bl_ctx* x, int id, int& kind) {
       kind = 2;
       return nnd;
     case BL_CPDENSITY: case BL_CPENERGY: case BL_CPPRESSURE: case BL_CPCS2: case BL_CPVOLUME:
+    case BL_FRVOLUME:  // changes only under the learned closure
       kind = ncp > 0 ? 3 : -1;
       return ncp;
     case BL_CNX: case BL_CNY:
@@ -1005,6 +1007,7 @@ static void* dev_ptr(bl_ctx* x, int id) {
     case BL_CPPRESSURE: return F.cpp;
     case BL_CPCS2: return F.cpcs2;
     case BL_CPVOLUME: return F.cpvol;
+    case BL_FRVOLUME: return F.frvol;
     default: return nullptr;
   }
 }
@@ -1098,19 +1101,20 @@ int bl_abi_sizes(int* out, int n) {
 // Several independent meshes (each one control file's problem) advanced
 // together: one kernel per phase over all of them, each mesh with its own
 // step header (dt, time, end test, errors).  The host arrays of the meshes
-// are concatenated into one disconnected mesh with node, element, region
-// and material numbers offset per mesh.
+// are concatenated into one disconnected mesh with node, element, region,
+// material, component and mixed-cell numbers offset per mesh.
 
 namespace {
 
-enum { kLayNone = 0, kLayEl, kLayCn, kLayNd, kLayEl4 };
-enum { kOffNone = 0, kOffNode, kOffEl, kOffReg, kOffMat };
+enum { kLayNone = 0, kLayEl, kLayCn, kLayNd, kLayEl4, kLayCp, kLayCp4, kLayMx };
+enum { kOffNone = 0, kOffNode, kOffEl, kOffReg, kOffMat, kOffCp };
 struct FieldLayout {
   int layout, off, is_int;
 };
 
-// How a dataAPI field concatenates: per element, per corner, per node or 4
-// per element, and the numbers its values hold.
+// How a dataAPI field concatenates: per element, per corner, per node, 4
+// per element, per component (1 or 4) or per mixed cell, and the numbers
+// its values hold.
 FieldLayout field_layout(int id) {
   switch (id) {
     case BL_ELDENSITY: case BL_ELENERGY: case BL_ELPRESSURE: case BL_ELCS2: case BL_ELVOLUME:
@@ -1136,14 +1140,36 @@ FieldLayout field_layout(int id) {
       return {kLayEl, kOffMat, 1};
     case BL_IELREG:
       return {kLayEl, kOffReg, 1};
+    case BL_CPDENSITY: case BL_CPENERGY: case BL_CPPRESSURE: case BL_CPCS2: case BL_CPVOLUME:
+    case BL_FRVOLUME: case BL_CPMASS: case BL_FRMASS: case BL_CPVISC: case BL_CPA1:
+    case BL_CPA3: case BL_CPB1: case BL_CPB3:
+      return {kLayCp, kOffNone, 0};
+    case BL_CPVISCX: case BL_CPVISCY:
+      return {kLayCp4, kOffNone, 0};
+    case BL_ICPMAT:
+      return {kLayCp, kOffMat, 1};
+    case BL_ICPNEXT: case BL_ICPPREV:
+      return {kLayCp, kOffCp, 1};
+    case BL_IMXEL:
+      return {kLayMx, kOffEl, 1};
+    case BL_IMXFCP:
+      return {kLayMx, kOffCp, 1};
+    case BL_IMXNCP:
+      return {kLayMx, kOffNone, 1};
     default:
       return {kLayNone, kOffNone, 0};
   }
 }
 
 size_t layout_count(int layout, const bl_sizes& s) {
-  return layout == kLayEl ? (size_t)s.nel
-                          : layout == kLayNd ? (size_t)s.nnd : 4 * (size_t)s.nel;
+  switch (layout) {
+    case kLayEl: return (size_t)s.nel;
+    case kLayNd: return (size_t)s.nnd;
+    case kLayCp: return (size_t)s.ncp;
+    case kLayCp4: return 4 * (size_t)s.ncp;
+    case kLayMx: return (size_t)s.nmx;
+    default: return 4 * (size_t)s.nel;
+  }
 }
 
 bool same_shared(const bl_config& a, const bl_config& b) {
@@ -1162,13 +1188,14 @@ void batch_copy(bl_ctx* x, int id, bool to_mesh) {
   const FieldLayout L = field_layout(id);
   if (L.layout == kLayNone || L.is_int || !x->host[id]) return;
   char* all = static_cast<char*>(x->host[id]);
+  const std::vector<int>& off = L.layout == kLayNd ? x->nd_off
+                                : (L.layout == kLayCp || L.layout == kLayCp4) ? x->cp_off
+                                : L.layout == kLayMx ? x->mx_off : x->el_off;
+  const size_t per = (L.layout == kLayCn || L.layout == kLayEl4 || L.layout == kLayCp4) ? 4 : 1;
   for (int i = 0; i < x->ninst; i++) {
     void* mine = x->inst_dh[i][id];
-    if (!mine) continue;
-    const size_t per = L.layout == kLayNd ? 1 : (L.layout == kLayEl ? 1 : 4);
-    const size_t b = (L.layout == kLayNd ? (size_t)x->nd_off[i] : (size_t)x->el_off[i]) * per;
-    const size_t n = (L.layout == kLayNd ? (size_t)(x->nd_off[i + 1] - x->nd_off[i])
-                                         : (size_t)(x->el_off[i + 1] - x->el_off[i])) * per;
+    const size_t b = (size_t)off[i] * per, n = (size_t)(off[i + 1] - off[i]) * per;
+    if (!mine || n == 0) continue;
     if (to_mesh) std::memcpy(mine, all + 8 * b, 8 * n);
     else std::memcpy(all + 8 * b, mine, 8 * n);
   }
@@ -1215,7 +1242,7 @@ int bl_init_batch(bl_ctx** out, int ninst, const bl_sizes* sizes, const bl_confi
   *out = nullptr;
   const bl_config& c0 = configs[0];
   std::vector<int> el_off(ninst + 1, 0), nd_off(ninst + 1, 0), reg_off(ninst + 1, 0),
-      mat_off(ninst + 1, 0);
+      mat_off(ninst + 1, 0), cp_off(ninst + 1, 0), mx_off(ninst + 1, 0);
   for (int i = 0; i < ninst; i++) {
     const bl_sizes& s = sizes[i];
     char msg[BL_SLEN + 1];
@@ -1225,8 +1252,8 @@ int bl_init_batch(bl_ctx** out, int ninst, const bl_sizes* sizes, const bl_confi
       set_err(error, BL_FAILURE, BL_HALT_ALL, msg);
       return BL_FAILURE;
     }
-    if (s.ncp != 0 || s.nmx != 0) {
-      std::snprintf(msg, sizeof msg, "ERROR: bl_init_batch: mesh %d has mixed cells", i + 1);
+    if (s.ncp < 0 || s.nmx < 0 || (s.ncp > 0) != (s.nmx > 0)) {
+      std::snprintf(msg, sizeof msg, "ERROR: bl_init_batch: mesh %d: mixed-cell sizes", i + 1);
       set_err(error, BL_FAILURE, BL_HALT_ALL, msg);
       return BL_FAILURE;
     }
@@ -1236,7 +1263,8 @@ int bl_init_batch(bl_ctx** out, int ninst, const bl_sizes* sizes, const bl_confi
       set_err(error, BL_FAILURE, BL_HALT_ALL, msg);
       return BL_FAILURE;
     }
-    if ((long long)el_off[i] + s.nel > 0x7fffffff || (long long)nd_off[i] + s.nnd > 0x7fffffff) {
+    if ((long long)el_off[i] + s.nel > 0x7fffffff || (long long)nd_off[i] + s.nnd > 0x7fffffff ||
+        (long long)cp_off[i] + s.ncp > 0x7fffffff) {
       set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init_batch: batch too large");
       return BL_FAILURE;
     }
@@ -1244,6 +1272,8 @@ int bl_init_batch(bl_ctx** out, int ninst, const bl_sizes* sizes, const bl_confi
     nd_off[i + 1] = nd_off[i] + s.nnd;
     reg_off[i + 1] = reg_off[i] + s.nreg;
     mat_off[i + 1] = mat_off[i] + s.nmat;
+    cp_off[i + 1] = cp_off[i] + s.ncp;
+    mx_off[i + 1] = mx_off[i] + s.nmx;
   }
   bl_sizes S{};
   S.nel = S.nel1 = S.nel2 = el_off[ninst];
@@ -1251,16 +1281,24 @@ int bl_init_batch(bl_ctx** out, int ninst, const bl_sizes* sizes, const bl_confi
   S.nsz = std::max(S.nel, S.nnd);
   S.nreg = reg_off[ninst];
   S.nmat = mat_off[ninst];
+  S.ncp = S.mcp = cp_off[ninst];
+  S.nmx = S.mmx = mx_off[ninst];
   // the concatenated host arrays
   std::vector<std::vector<char>> store(BL_NID + 1);
   std::vector<void*> cdh(BL_NID + 1, nullptr);
   for (int id = 1; id <= BL_NID; id++) {
     const FieldLayout L = field_layout(id);
     if (L.layout == kLayNone) continue;
-    int have = 0;
-    for (int i = 0; i < ninst; i++) have += dh[i][id] != nullptr;
+    // a field is registered by every mesh that has entries of it (a mesh
+    // without mixed cells need not register the component fields)
+    int have = 0, need = 0;
+    for (int i = 0; i < ninst; i++) {
+      const bool some = layout_count(L.layout, sizes[i]) > 0;
+      need += some;
+      have += some && dh[i][id] != nullptr;
+    }
     if (have == 0) continue;
-    if (have != ninst) {
+    if (have != need) {
       char msg[BL_SLEN + 1];
       std::snprintf(msg, sizeof msg, "ERROR: bl_init_batch: field %d registered for some meshes only",
                     id);
@@ -1272,13 +1310,16 @@ int bl_init_batch(bl_ctx** out, int ninst, const bl_sizes* sizes, const bl_confi
     size_t at = 0;
     for (int i = 0; i < ninst; i++) {
       const size_t n = layout_count(L.layout, sizes[i]);
+      if (n == 0) continue;
       std::memcpy(store[id].data() + esz * at, dh[i][id], esz * n);
       if (L.is_int && L.off != kOffNone) {
         int* v = reinterpret_cast<int*>(store[id].data()) + at;
         const int add = L.off == kOffNode ? nd_off[i] : L.off == kOffEl ? el_off[i]
-                      : L.off == kOffReg ? reg_off[i] : mat_off[i];
-        for (size_t k = 0; k < n; k++)
+                      : L.off == kOffReg ? reg_off[i] : L.off == kOffCp ? cp_off[i] : mat_off[i];
+        for (size_t k = 0; k < n; k++) {
           if (L.off == kOffNode || L.off == kOffEl || v[k] > 0) v[k] += add;
+          else if (id == BL_IELMAT && v[k] < 0) v[k] -= mx_off[i];  // -(mixed cell)
+        }
       }
       at += n;
     }
@@ -1310,6 +1351,8 @@ int bl_init_batch(bl_ctx** out, int ninst, const bl_sizes* sizes, const bl_confi
   x->el_off = el_off;
   x->nd_off = nd_off;
   x->mat_off = mat_off;
+  x->cp_off = cp_off;
+  x->mx_off = mx_off;
   x->inst_dh.resize(ninst);
   for (int i = 0; i < ninst; i++) x->inst_dh[i].assign(dh[i], dh[i] + BL_NID + 1);
   // per-mesh controls and ownership tables
@@ -1410,6 +1453,7 @@ int bl_run_batch(bl_ctx* x, bl_timestep* ts, int max_steps, int* status, int* ns
     x->L.lag_force_b(F, C, x->stream);
     x->L.lag_accel_b(F, C, x->stream);
     x->L.lag_state_b(F, C, x->stream);
+    x->L.mix_closure_b(F, C, x->stream);
     if (with_ale) x->L.ale_b(F, C, x->stream);
   };
   if (!x->bexec || x->b_ale != with_ale || x->b_gsteps != G || x->b_ndblock != F.nd_block) {
@@ -1490,8 +1534,8 @@ const float* bl_mlp_device_image(bl_mlp* m);  // bl_mlp.cu
 
 int bl_set_closure(bl_ctx* x, bl_mlp* net, const float* norm, int on, bl_error* e) {
   set_err(e, BL_SUCCESS, BL_HALT_SINGLE, "");
-  if (!x || (on && (!net || !norm)) || x->ninst > 0) {
-    set_err(e, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_set_closure: bad argument (or a batch context)");
+  if (!x || (on && (!net || !norm))) {
+    set_err(e, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_set_closure: bad argument");
     return BL_FAILURE;
   }
   bl::DevFields& F = x->F;
@@ -1510,9 +1554,11 @@ int bl_set_closure(bl_ctx* x, bl_mlp* net, const float* norm, int on, bl_error* 
                     cudaMemcpyDeviceToDevice, x->stream);
   }
   F.closure = on ? 1 : 0;
-  // the device loop's graph holds the old arguments
+  // the device loops' graphs hold the old arguments
   if (x->gexec) cudaGraphExecDestroy(x->gexec);
   x->gexec = nullptr;
+  if (x->bexec) cudaGraphExecDestroy(x->bexec);
+  x->bexec = nullptr;
   return cudaStreamSynchronize(x->stream) == cudaSuccess ? BL_SUCCESS : BL_FAILURE;
 }
 

@@ -36,6 +36,7 @@ struct bl_ctx {
   // a batch of meshes (bl_init_batch); ninst = 0 for a single mesh
   int ninst = 0;
   std::vector<int> el_off, nd_off, mat_off;    // [ninst+1] first element, node, material
+  std::vector<int> cp_off, mx_off;             // [ninst+1] first component, mixed cell
   bl::DevStep* hsteps = nullptr;               // pinned mirror of F.steps
   std::vector<bl::DevInst> inst_h;             // host copy of the per-mesh controls
   std::vector<std::vector<void*>> inst_dh;     // each mesh's registered host arrays

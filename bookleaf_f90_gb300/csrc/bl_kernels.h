@@ -26,6 +26,7 @@ namespace bl {
   void launch_ale_batch(const DevFields& F, const DevCfg& C, cudaStream_t s);      \
   int prepare_mix_closure();                                                       \
   void launch_mix_closure(const DevFields& F, const DevCfg& C, cudaStream_t s);    \
+  void launch_mix_closure_batch(const DevFields& F, const DevCfg& C, cudaStream_t s);\
   }
 
 BL_DECLARE_LAUNCHERS(fast)
@@ -47,6 +48,7 @@ struct Launchers {
   // the learned mixed-cell closure (after lag_state; no-op when off)
   int (*mix_prepare)();
   void (*mix_closure)(const DevFields&, const DevCfg&, cudaStream_t);
+  void (*mix_closure_b)(const DevFields&, const DevCfg&, cudaStream_t);
 };
 
 // Kernels launched by one call of each launcher (for bl_kernel_launches).

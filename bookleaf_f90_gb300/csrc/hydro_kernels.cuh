@@ -1464,11 +1464,12 @@ __global__ void BL_STATE_BOUNDS(BS) k_lag_state(DevFields F, DevCfg C) {
 // closure's work, and the exchanged volume trades energy at the mixture
 // pressure fr_1 p_1 + fr_2 p_2, which sums to zero over the cell: the cell's
 // total energy, like its volume and every element and node field, is the
-// plain closure's, and a rejected cell ends exactly as under it.
+// plain closure's, and a rejected cell ends exactly as under it.  In a
+// batch each cell reads the step header of its own mesh.
 constexpr int kClosureWarps = 4;
+template <bool BATCH>
 __global__ void __launch_bounds__(32 * kClosureWarps) k_mix_closure(DevFields F, DevCfg C) {
-  const DevStep* S = F.step;
-  if (halted(S)) return;
+  if (!BATCH && halted(F.step)) return;
   extern __shared__ unsigned char smem[];
   mlp::SmemW& w = *reinterpret_cast<mlp::SmemW*>(smem);
   mlp::SmemS* Ss = reinterpret_cast<mlp::SmemS*>(smem + sizeof(mlp::SmemW));
@@ -1477,15 +1478,17 @@ __global__ void __launch_bounds__(32 * kClosureWarps) k_mix_closure(DevFields F,
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   mlp::SmemS& s = Ss[warp];
   const int imx = blockIdx.x * (16 * kClosureWarps) + warp * 16 + (lane & 15);
-  const bool cell = lane < 16 && imx < F.nmx && F.imxncp[imx] == 2;
-  const double dt = S->dt;
+  const bool two = lane < 16 && imx < F.nmx && F.imxncp[imx] == 2;
+  const int iel = two ? F.imxel[imx] : 0;
+  const DevStep* S = el_step<BATCH>(F, iel);
+  const bool cell = two && !halted(S);
+  const double dt = cell ? S->dt : 0.0;
   double V0 = 0.0, V1 = 0.0;
-  int c0 = 0, iel = 0;
+  int c0 = 0;
   if (lane < 16) {
     float f[mlp::NI];
     if (cell) {
       c0 = F.imxfcp[imx];
-      iel = F.imxel[imx];
       V0 = F.mxv0[imx];
       V1 = F.vol[iel];
       const double p1 = F.cpp[c0], p2 = F.cpp[c0 + 1];
@@ -1590,13 +1593,22 @@ void launch_lag_state(const DevFields& F, const DevCfg& C, cudaStream_t s) {
 }
 constexpr size_t kClosureSmem = sizeof(mlp::SmemW) + kClosureWarps * sizeof(mlp::SmemS);
 int prepare_mix_closure() {
-  return cudaFuncSetAttribute(k_mix_closure, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)kClosureSmem) == cudaSuccess ? 0 : -1;
+  return cudaFuncSetAttribute(k_mix_closure<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)kClosureSmem) == cudaSuccess &&
+                 cudaFuncSetAttribute(k_mix_closure<true>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kClosureSmem) == cudaSuccess
+             ? 0 : -1;
 }
 void launch_mix_closure(const DevFields& F, const DevCfg& C, cudaStream_t s) {
   if (!F.closure || F.nmx < 1) return;
   const int per = 16 * kClosureWarps;
-  k_mix_closure<<<(F.nmx + per - 1) / per, 32 * kClosureWarps, kClosureSmem, s>>>(F, C);
+  k_mix_closure<false><<<(F.nmx + per - 1) / per, 32 * kClosureWarps, kClosureSmem, s>>>(F, C);
+}
+void launch_mix_closure_batch(const DevFields& F, const DevCfg& C, cudaStream_t s) {
+  if (!F.closure || F.nmx < 1) return;
+  const int per = 16 * kClosureWarps;
+  k_mix_closure<true><<<(F.nmx + per - 1) / per, 32 * kClosureWarps, kClosureSmem, s>>>(F, C);
 }
 // a batch of meshes: k_getdt over each mesh's own blocks, the rest over all
 // elements or nodes, each reading the step header of its mesh

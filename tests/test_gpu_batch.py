@@ -123,3 +123,68 @@ def test_autotuned_batch_still_equals_each_mesh_alone():
         assert _same_timestep(p.timestep, q.timestep)
         assert not compare(p, q, exact=True)
     b.close()
+
+
+# two-material tubes (mixed cells along a tilted interface) of different
+# sizes, tilts and states, and a pure Sod tube
+def _two_material(nx, tilt, st, time_end=0.02):
+    deck, frac = configs.sod_interface(nx, nx // 10, time_end=time_end, amplitude=0.0, periods=0,
+                                       tilt=tilt, rho_right=st, p_right=st)
+    return Problem.from_deck(deck, material_fraction=frac)
+
+
+def _mixed_problems():
+    return [_two_material(80, 0.2, 0.5), _two_material(64, 0.3, 0.6, 0.015),
+            Problem.from_deck(configs.sod(24, 4, time_end=0.02)),
+            _two_material(96, 0.1, 0.4, 0.025)]
+
+
+def _closure_net():
+    from bookleaf_f90_gb300 import closure
+    import numpy as np
+    # an untrained network: its exchanges are arbitrary, within the
+    # admissible range, which is all the batch comparison needs
+    net = closure.ClosureNet(seed=3)
+    norm = np.concatenate([[0.5, 1, 0.5, 1, 0.5, 1.4, 1.5, 0, 0.1, 0.3],
+                           [3, 2, 3, 2, 3, 2, 2, 300, 5, 2], [1e-3, 10.0]])
+    return net, norm
+
+
+@pytest.mark.parametrize("learned", [False, True], ids=["plain", "learned"])
+@pytest.mark.parametrize("fp", [abi.FP_EXACT, abi.FP_FAST], ids=["exact", "fast"])
+def test_batch_with_mixed_cells_equals_each_mesh_alone(fp, learned):
+    """Meshes with mixed cells concatenate with their component and
+    mixed-cell numbers offset; under the plain or the learned closure each
+    ends as it does alone, bit for bit, and the closure sees the same cells."""
+    net, norm = _closure_net() if learned else (None, None)
+    probs = _mixed_problems()
+    b = BatchSolver(probs, fp_mode=fp)
+    if learned:
+        b.set_closure(net, norm)
+    ierr, status, _ = b.run()
+    assert ierr == 0 and status == [0] * len(probs), b.error.message
+    b.sync_to_host(0)
+    seen_b = b.closure_stats()
+    b.close()
+    seen = [0, 0]
+    for i, q in enumerate(_mixed_problems()):
+        s = Solver(q, fp_mode=fp)
+        if learned:
+            s.set_closure(net, norm)
+        ierr, _ = s.run(history=False)
+        assert ierr == 0, s.error.message
+        s.sync_to_host(0)
+        st = s.closure_stats()
+        seen[0] += st[0]
+        seen[1] += st[1]
+        s.close()
+        p = probs[i]
+        assert _same_timestep(p.timestep, q.timestep), (i, p.timestep.as_tuple(), q.timestep.as_tuple())
+        assert not compare(p, q, exact=True), i
+        if q.sizes.ncp:
+            for fid in (abi.CPVOLUME, abi.CPENERGY, abi.CPDENSITY, abi.FRVOLUME):
+                assert (p.fields[fid] == q.fields[fid]).all(), (i, abi.NAMES[fid])
+    assert tuple(seen) == seen_b
+    if learned:
+        assert seen_b[0] > 0 and seen_b[1] < seen_b[0]
+        net.close()
