@@ -67,11 +67,11 @@ class BatchSolver:
         cand = [(G, B) for G in (8, 16, 32) for B in (128, 256, 512)]
         return g.value, bs.value, dict(zip(cand, list(ms)))
 
-    def set_closure(self, net, norm, on=True):
+    def set_closure(self, net, norm, on=True, volume_only=False):
         """The learned mixed-cell closure for every mesh of the batch (see
         Solver.set_closure)."""
         from .solver import Solver
-        Solver.set_closure(self, net, norm, on)
+        Solver.set_closure(self, net, norm, on, volume_only)
 
     def closure_stats(self):
         """(mixed-cell steps the closure saw, those it left to the plain

@@ -1534,7 +1534,7 @@ const float* bl_mlp_device_image(bl_mlp* m);  // bl_mlp.cu
 
 int bl_set_closure(bl_ctx* x, bl_mlp* net, const float* norm, int on, bl_error* e) {
   set_err(e, BL_SUCCESS, BL_HALT_SINGLE, "");
-  if (!x || (on && (!net || !norm))) {
+  if (!x || on < 0 || on > 2 || (on && (!net || !norm))) {
     set_err(e, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_set_closure: bad argument");
     return BL_FAILURE;
   }
@@ -1553,7 +1553,7 @@ int bl_set_closure(bl_ctx* x, bl_mlp* net, const float* norm, int on, bl_error* 
     cudaMemcpyAsync(F.mlp_img, bl_mlp_device_image(net), bl::mlp::kImgN * sizeof(float),
                     cudaMemcpyDeviceToDevice, x->stream);
   }
-  F.closure = on ? 1 : 0;
+  F.closure = on;
   // the device loops' graphs hold the old arguments
   if (x->gexec) cudaGraphExecDestroy(x->gexec);
   x->gexec = nullptr;

@@ -129,7 +129,8 @@ struct DevFields {
   const int* blkinst;        // [nblk_batch] mesh of a k_getdt block
   int ninst, nblk_batch;
   int nd_block;              // block size of the batch's node kernels (autotuned)
-  // learned mixed-cell closure (bl_set_closure; off when closure == 0)
+  // learned mixed-cell closure (bl_set_closure): 0 off, 1 volume and energy
+  // exchange, 2 volume only
   int closure;
   float* mlp_img;            // the network's parameters as their shared-memory
                              // image (bl_mma.cuh), copied at bl_set_closure

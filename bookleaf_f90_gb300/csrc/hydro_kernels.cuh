@@ -1461,11 +1461,15 @@ __global__ void BL_STATE_BOUNDS(BS) k_lag_state(DevFields F, DevCfg C) {
 // conservation (|y_1 + y_2| > norm[21]), lie out of range (farther than
 // |x_eq| outside [0, x_eq]) or leave a material a non-positive volume;
 // F.mlp_count[1] counts those cells.  Each material's energy takes the plain
-// closure's work, and the exchanged volume trades energy at the mixture
-// pressure fr_1 p_1 + fr_2 p_2, which sums to zero over the cell: the cell's
-// total energy, like its volume and every element and node field, is the
-// plain closure's, and a rejected cell ends exactly as under it.  In a
-// batch each cell reads the step header of its own mesh.
+// closure's work; with F.closure == 1 the exchanged volume also trades
+// energy at the mixture pressure fr_1 p_1 + fr_2 p_2 (the work one material
+// does on the other, summing to zero over the cell), with F.closure == 2
+// the materials keep their specific energies, so that for ideal gases the
+// cell's mixture pressure sum (gamma_m - 1) E_m / V, and with it every later
+// element and node field, stays the plain closure's.  Either way the cell's
+// volume and total energy, and every element and node field of the step,
+// are the plain closure's, and a rejected cell ends exactly as under it.
+// In a batch each cell reads the step header of its own mesh.
 constexpr int kClosureWarps = 4;
 template <bool BATCH>
 __global__ void __launch_bounds__(32 * kClosureWarps) k_mix_closure(DevFields F, DevCfg C) {
@@ -1555,7 +1559,7 @@ __global__ void __launch_bounds__(32 * kClosureWarps) k_mix_closure(DevFields F,
     if (ok) {
       const double cpm = F.cpm[icp];
       cpv = pv[k] + x[k] * V0;
-      cpe = pe[k] - DIV(pbar * (x[k] * V0), maxF(cpm, zc));
+      if (F.closure == 1) cpe = pe[k] - DIV(pbar * (x[k] * V0), maxF(cpm, zc));
       cpr = DIV(cpm, cpv);
       eos_pc(C, __ldg(F.icpmat + icp), cpr, cpe, cpp, cpc);
       F.frvol[icp] = DIV(cpv, V1);

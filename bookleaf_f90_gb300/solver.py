@@ -127,17 +127,21 @@ class Solver:
         return ierr, list(ms)
 
     # ---- the learned mixed-cell closure -------------------------------------
-    def set_closure(self, net, norm, on=True):
+    def set_closure(self, net, norm, on=True, volume_only=False):
         """Let the network net (closure.ClosureNet; its current parameters
         are copied) split each two-material cell's volume change between its
         materials from the next Lagrangian step on, with the feature
         standardisation norm (22 floats, see closure.fit_norm); on=False
-        restores the plain closure."""
+        restores the plain closure.  By default the moved volume trades
+        energy at the mixture pressure; with volume_only the materials keep
+        their specific energies and, for ideal gases, the flow stays the
+        plain closure's (only the split between the materials changes)."""
         nm_arr = np.ascontiguousarray(norm, dtype=np.float32) if on else None
         if on and nm_arr.size != 22:
             raise ValueError("norm needs 22 floats")
         nm = nm_arr.ctypes.data_as(ct.c_void_p) if on else None
-        if self.L.bl_set_closure(self.ctx, net.handle if on else None, nm, int(bool(on)),
+        mode = (2 if volume_only else 1) if on else 0
+        if self.L.bl_set_closure(self.ctx, net.handle if on else None, nm, mode,
                                  ct.byref(self.error)) != 0:
             raise SolverError(-1, self.error.iout, self.error.message)
 

@@ -274,10 +274,14 @@ int bl_mlp_train(bl_mlp *m, const float *x, const float *t, int n, int epochs, i
  * materials towards pressure equilibrium and not past it.  A cell whose
  * outputs are not finite, do not cancel within norm[21] (volume
  * conservation), lie farther outside that range than its width, or leave a
- * material a non-positive volume keeps the plain closure.  The exchanged
- * volume trades energy at the mixture pressure, so each cell's volume and
- * total energy, and every element and node field, are the plain closure's.
- * on = 0 restores the plain closure everywhere.  Not for batch contexts. */
+ * material a non-positive volume keeps the plain closure.  on = 1: the
+ * exchanged volume trades energy at the mixture pressure (the work one
+ * material does on the other); on = 2: the materials keep their specific
+ * energies, so that for ideal gases the cell's mixture pressure, and with
+ * it every element and node field of the run, stays the plain closure's.
+ * Either way each cell's volume and total energy are the plain closure's.
+ * on = 0 restores the plain closure everywhere.  On a batch context it
+ * applies to every mesh. */
 int bl_set_closure(bl_ctx *ctx, bl_mlp *net, const float *norm, int on, bl_error *err);
 /* cells the closure has seen and cells it handed back to the plain closure */
 int bl_closure_stats(bl_ctx *ctx, unsigned long long *cells, unsigned long long *rejected);

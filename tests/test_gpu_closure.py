@@ -41,10 +41,10 @@ def _problem(case, nx=NX, ny=NY):
     return Problem.from_deck(deck, material_fraction=frac)
 
 
-def _run(p, fp, net=None, norm=None):
+def _run(p, fp, net=None, norm=None, volume_only=False):
     s = Solver(p, fp_mode=fp)
     if net is not None:
-        s.set_closure(net, norm)
+        s.set_closure(net, norm, volume_only=volume_only)
     ierr, _ = s.run(history=False)
     assert ierr == 0, s.error.message
     s.sync_to_host(0)
@@ -166,3 +166,27 @@ def test_learned_closure_beats_the_plain_closure_on_an_unseen_interface(trained)
     ep = closure.cell_density_error(runs["plain"], idx, truth, cells)
     el = closure.cell_density_error(runs["learned"], idx, truth, cells)
     assert l1_mixed < 0.1 * ep and el < ep, (l1_mixed, ep, el)
+
+
+def test_volume_only_closure_keeps_the_plain_flow_and_still_gains(trained):
+    """With the materials keeping their specific energies the cells' mixture
+    pressures, and so every element and node field of the whole run, stay
+    the plain closure's (to rounding): the benchmark spec's bar of 1e-3 on the
+    mixed cells' density against the plain closure is met by construction,
+    while the split between the materials still moves towards the refined
+    run's."""
+    net, norm = trained[:2]
+    _, _, truth = closure.subcell_samples(functools.partial(_make, TEST), NX, NY, lags=(1,))
+    pp, pv = _problem(TEST), _problem(TEST)
+    idx = closure.grid_index(pp, NX, NY)
+    cells = idx[pp.fields[abi.IMXEL][:pp.sizes.nmx] - 1]
+    _run(pp, abi.FP_FAST)
+    (seen, rejected), _ = _run(pv, abi.FP_FAST, net, norm, volume_only=True)
+    assert pv.timestep.nstep == pp.timestep.nstep and rejected < 0.5 * seen
+    for fid in (abi.ELDENSITY, abi.ELENERGY, abi.ELPRESSURE, abi.NDX, abi.NDY, abi.NDU, abi.NDV):
+        assert np.allclose(pv.fields[fid], pp.fields[fid], rtol=1e-10, atol=1e-13), abi.NAMES[fid]
+    shift, l1_mixed, l1_all = closure.against_plain(pv, pp, idx, NX, NY)
+    assert shift < 1.0 and l1_mixed < 1e-3 and l1_all < 1e-3, (shift, l1_mixed, l1_all)
+    (fp, r1p, r2p) = closure.mixed_errors(pp, idx, truth, cells)
+    (fv, r1v, r2v) = closure.mixed_errors(pv, idx, truth, cells)
+    assert fv < 0.7 * fp and r1v < 0.7 * r1p and r2v < 0.7 * r2p, ((fp, r1p, r2p), (fv, r1v, r2v))
