@@ -70,7 +70,10 @@ __device__ __forceinline__ void store_c(const float (&c)[4], FS s) {
   s(g + 8, 2 * t + 1, c[3]);
 }
 
-__device__ __forceinline__ float sigm(float z) { return 1.0f / (1.0f + __expf(-z)); }
+// the logistic function with the fast single-precision divide: its error of
+// a few ulp is far below the BF16 rounding every activation goes through,
+// and for z below about -87 it gives the limit 0
+__device__ __forceinline__ float sigm(float z) { return __fdividef(1.0f, 1.0f + __expf(-z)); }
 
 // The parameters in shared memory, zero-padded to whole tiles: W1 as 64x16,
 // W3 as 16x64.
@@ -126,12 +129,12 @@ static __device__ void forward_warp(const SmemW& w, SmemS& s) {
     uint32_t b[2];
     frag_b(b, [&](int k, int n) { return w.w1[nt * 8 + n][k]; });
     mma16816(d, a, b);
-    store_c(d, [&](int r, int c, float v) { s.z1[r][nt * 8 + c] = v + w.b1[nt * 8 + c]; });
-  }
-  __syncwarp();
-  for (int i = threadIdx.x & 31; i < 16 * NH; i += 32) {
-    const float z = s.z1[i / NH][i % NH];
-    s.h1[i / NH][i % NH] = z * sigm(z);
+    // the activation straight from the accumulators (z kept for the backward pass)
+    store_c(d, [&](int r, int c, float v) {
+      const float z = v + w.b1[nt * 8 + c];
+      s.z1[r][nt * 8 + c] = z;
+      s.h1[r][nt * 8 + c] = z * sigm(z);
+    });
   }
   __syncwarp();
   // layer 2: z2 = h1 W2^T + b2 (K = 64, N = 64)
@@ -145,12 +148,11 @@ static __device__ void forward_warp(const SmemW& w, SmemS& s) {
       frag_b(b, [&](int k, int n) { return w.w2[nt * 8 + n][kt * 16 + k]; });
       mma16816(d, a, b);
     }
-    store_c(d, [&](int r, int c, float v) { s.z2[r][nt * 8 + c] = v + w.b2[nt * 8 + c]; });
-  }
-  __syncwarp();
-  for (int i = threadIdx.x & 31; i < 16 * NH; i += 32) {
-    const float z = s.z2[i / NH][i % NH];
-    s.h2[i / NH][i % NH] = z * sigm(z);
+    store_c(d, [&](int r, int c, float v) {
+      const float z = v + w.b2[nt * 8 + c];
+      s.z2[r][nt * 8 + c] = z;
+      s.h2[r][nt * 8 + c] = z * sigm(z);
+    });
   }
   __syncwarp();
   // layer 3: y = h2 W3^T + b3 (K = 64, N = 8 of which NO used)
