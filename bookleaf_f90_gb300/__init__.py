@@ -10,7 +10,6 @@
   build    nvcc build of the in-tree shared library
 """
 from . import abi  # noqa: F401
-from . import closure  # noqa: F401
 from .solver import Solver, SolverError  # noqa: F401
 from .batch import BatchSolver  # noqa: F401
 from .setup import Problem, configs  # noqa: F401
