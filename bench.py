@@ -302,6 +302,10 @@ def run_ensemble(args, torch):
 # hourglass control; the line records where.
 CLOSURE_TRAIN = [(t, s) for t in (0.1, 0.3, 0.4) for s in (0.5, 0.6)] + [(0.1, 0.4), (0.3, 0.4)]
 CLOSURE_TEST = (0.2, 0.5)
+# the coarse meshes of the training runs, with their cases (at 320x32 the
+# refined run of tilt 0.3, state 0.4 stops with dt < dt_min)
+CLOSURE_TRAIN_MESHES = [((160, 16), CLOSURE_TRAIN),
+                        ((320, 32), [c for c in CLOSURE_TRAIN if c != (0.3, 0.4)])]
 
 
 def _closure_case(case, nx, ny, time_end=0.2):
@@ -315,8 +319,8 @@ def run_closure(args, torch):
     """The learned mixed-cell closure (--workload closure; --size = cells
     across the tube, default 800, with size / 10 rows; the 4x-refined plain
     run stops with dt < dt_min from 4800 cells across): the network is
-    trained on the GPU on sub-cell data of 4x-refined plain runs (160x16
-    meshes, eight interfaces), then the held-out interface is run to t = 0.2
+    trained on the GPU on sub-cell data of 4x-refined plain runs (160x16 and
+    320x32 meshes, CLOSURE_TRAIN_MESHES), then the held-out interface is run to t = 0.2
     with the plain and with the learned closure, and 4x refined with the
     plain closure (the sub-cell truth, and the cost the coarse learned run
     replaces).  Each run is timed whole with CUDA events on its stream after
@@ -329,11 +333,12 @@ def run_closure(args, torch):
     W = max(1, args.warmup)
     t0 = time.perf_counter()
     Xs, Ds = [], []
-    for case in CLOSURE_TRAIN:
-        X, D, _ = closure.subcell_samples(functools.partial(_closure_case, case), 160, 16,
-                                          fp_mode=fp)
-        Xs.append(X)
-        Ds.append(D)
+    for (tx, ty), train_cases in CLOSURE_TRAIN_MESHES:
+        for case in train_cases:
+            X, D, _ = closure.subcell_samples(functools.partial(_closure_case, case), tx, ty,
+                                              fp_mode=fp)
+            Xs.append(X)
+            Ds.append(D)
     X, D = np.concatenate(Xs), np.concatenate(Ds)
     t1 = time.perf_counter()
     net, norm, losses = closure.train(X, D, epochs=100)
@@ -439,8 +444,11 @@ def run_closure(args, torch):
                                     % CLOSURE_TEST,
                        "timed": "t = 0 to 0.2, %d steps" % rl["steps"],
                        "network": "10-64-64-2 SiLU, BF16 operands, FP32 accumulation",
-                       "training": {"samples": int(len(X)), "cases": len(CLOSURE_TRAIN),
-                                    "mesh": "160x16, 4x refined", "epochs": 100,
+                       "training": {"samples": int(len(X)),
+                                    "cases": sum(len(c) for _, c in CLOSURE_TRAIN_MESHES),
+                                    "mesh": " and ".join("%dx%d" % m for m, _ in
+                                                         CLOSURE_TRAIN_MESHES) + ", 4x refined",
+                                    "epochs": 100,
                                     "loss_first_last": [float(losses[0]), float(losses[-1])],
                                     "data_s": t1 - t0, "train_s": t2 - t1}},
             "plain_closure": {"value": rp["rate"], "unit": "zone-cycles/s", "ms": rp["ms"],
@@ -506,11 +514,12 @@ def run_closure_ensemble(args, torch):
         cases.append((max(10, nx), float(rng.uniform(0.1, 0.4)), float(rng.uniform(0.5, 0.6))))
     t0 = time.perf_counter()
     Xs, Ds = [], []
-    for case in CLOSURE_TRAIN:
-        X, D, _ = closure.subcell_samples(functools.partial(_closure_case, case), 160, 16,
-                                          fp_mode=fp)
-        Xs.append(X)
-        Ds.append(D)
+    for (tx, ty), train_cases in CLOSURE_TRAIN_MESHES:
+        for case in train_cases:
+            X, D, _ = closure.subcell_samples(functools.partial(_closure_case, case), tx, ty,
+                                              fp_mode=fp)
+            Xs.append(X)
+            Ds.append(D)
     net, norm, losses = closure.train(np.concatenate(Xs), np.concatenate(Ds), epochs=100)
     train_s = time.perf_counter() - t0
 

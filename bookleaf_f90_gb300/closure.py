@@ -186,11 +186,16 @@ def subcell_samples(make, nx, ny, refine=4, lags=(1, 2, 4), fp_mode=abi.FP_FAST,
     try:
         s.sync_to_host(0)
         hist = [material_sums(pf, index, ncell) + (pf.timestep.time,)]
+        # masses never change: after the first download only the volumes
+        # and energies are read back
+        moving = (abi.ELVOLUME, abi.ELENERGY) + ((abi.CPVOLUME, abi.CPENERGY)
+                                                 if pf.sizes.ncp > 0 else ())
         while pf.timestep.time < pf.config.time_end:
             ierr, _ = s.run(max_steps=1, history=False)
             if ierr != 0:
                 raise RuntimeError("fine run failed: " + s.error.message)
-            s.sync_to_host(0)
+            for fid in moving:
+                s.sync_to_host(fid)
             cur = material_sums(pf, index, ncell) + (pf.timestep.time,)
             hist = (hist + [cur])[-(max(lags) + 1):]
             for lag in lags:
