@@ -156,7 +156,7 @@ def test_learned_closure_beats_the_plain_closure_on_an_unseen_interface(trained)
     assert stats[1] < 0.3 * stats[0], stats
     assert fl < 0.5 * fp, errs
     assert r1l < 0.5 * r1p and r2l < 0.5 * r2p, errs
-    # and the plain closure, as the judge, sees the same flow: the interface
+    # and against the plain closure, the reference, the flow is the same: the interface
     # within one cell of its own in every row and the densities within 1e-3
     # (relative L1 over the mesh).  Over the mixed cells alone the densities
     # move by much less than the plain closure's own error there against
@@ -174,8 +174,8 @@ def test_learned_closure_beats_the_plain_closure_on_an_unseen_interface(trained)
 def test_volume_only_closure_keeps_the_plain_flow_and_still_gains(trained):
     """With the materials keeping their specific energies the cells' mixture
     pressures, and so every element and node field of the whole run, stay
-    the plain closure's (to rounding): the benchmark spec's bar of 1e-3 on the
-    mixed cells' density against the plain closure is met by construction,
+    the plain closure's (to rounding): a bar of 1e-3 on the mixed cells'
+    density against the plain closure is met by construction,
     while the split between the materials still moves towards the refined
     run's."""
     net, norm = trained[:2]

@@ -2,9 +2,8 @@
 
 Exact mode (BL_FP_EXACT, no fused multiply-add) must reproduce the
 restatement bit for bit after every solver call.  Fast mode (FMA allowed)
-must stay within the stated tolerances of the reference's north-star
-criteria: total mass and energy to 1e-12 relative and density, energy and
-velocity fields within 1e-9 L1 relative.
+must stay within these tolerances of it: total mass and energy to 1e-12
+relative and density, energy and velocity fields within 1e-9 L1 relative.
 """
 import numpy as np
 import pytest
