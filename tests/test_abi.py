@@ -67,3 +67,15 @@ def test_init_rejects_bad_connectivity(lib):
                        ct.cast(tab, ct.c_void_p), 0, ct.byref(err))
     assert ierr == abi.FAILURE
     assert "out of range" in err.message or "CUDA" in err.message
+
+
+def test_closure_entry_points_reject_bad_arguments(lib):
+    """bl_set_closure / bl_closure_stats check their arguments before any
+    CUDA call: no context, an unknown mode, or a mode without a network."""
+    err = abi.Error()
+    norm = (ct.c_float * 22)()
+    assert lib.bl_set_closure(None, None, None, 0, ct.byref(err)) == abi.FAILURE
+    assert "bad argument" in err.message
+    assert lib.bl_set_closure(None, None, norm, 3, ct.byref(err)) == abi.FAILURE
+    a, b = ct.c_ulonglong(7), ct.c_ulonglong(7)
+    assert lib.bl_closure_stats(None, ct.byref(a), ct.byref(b)) == abi.FAILURE
