@@ -1482,94 +1482,100 @@ __global__ void __launch_bounds__(32 * kClosureWarps) k_mix_closure(DevFields F,
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   mlp::SmemS& s = Ss[warp];
   const int imx = blockIdx.x * (16 * kClosureWarps) + warp * 16 + (lane & 15);
-  const bool two = lane < 16 && imx < F.nmx && F.imxncp[imx] == 2;
+  // lanes l and l + 16 share cell l: the features and the network take one
+  // row per cell (lanes 0-15), the FP64 update one material per lane
+  const int k = lane >> 4;
+  const bool two = imx < F.nmx && F.imxncp[imx] == 2;
   const int iel = two ? F.imxel[imx] : 0;
   const DevStep* S = el_step<BATCH>(F, iel);
   const bool cell = two && !halted(S);
   const double dt = cell ? S->dt : 0.0;
   double V0 = 0.0, V1 = 0.0;
   int c0 = 0;
+  if (cell) {
+    c0 = F.imxfcp[imx];
+    V0 = F.mxv0[imx];
+    V1 = F.vol[iel];
+  }
   if (lane < 16) {
     float f[mlp::NI];
     if (cell) {
-      c0 = F.imxfcp[imx];
-      V0 = F.mxv0[imx];
-      V1 = F.vol[iel];
       const double p1 = F.cpp[c0], p2 = F.cpp[c0 + 1];
       const double q1 = F.cpcs2[c0], q2 = F.cpcs2[c0 + 1];
       const double raw[mlp::NI] = {F.frvol[c0], F.cprho[c0], F.cprho[c0 + 1], p1, p2, q1, q2,
                                    (V1 - V0) / V0, dt * sqrt(maxF(q1, q2) / V0),
                                    (p1 - p2) / (absF(p1) + absF(p2) + 1e-300)};
 #pragma unroll
-      for (int k = 0; k < mlp::NI; k++)
-        f[k] = ((float)raw[k] - __ldg(F.mlp_norm + k)) * __ldg(F.mlp_norm + mlp::NI + k);
+      for (int j = 0; j < mlp::NI; j++)
+        f[j] = ((float)raw[j] - __ldg(F.mlp_norm + j)) * __ldg(F.mlp_norm + mlp::NI + j);
     }
 #pragma unroll
-    for (int k = 0; k < 16; k++) s.x[lane][k] = (cell && k < mlp::NI) ? f[k] : 0.0f;
+    for (int j = 0; j < 16; j++) s.x[lane][j] = (cell && j < mlp::NI) ? f[j] : 0.0f;
   }
   __syncwarp();
   mlp::forward_warp(w, s);
-  if (!cell) return;
+  // this lane's material: the plain closure's step (k_lag_state's component
+  // update), the fallback and the state the admissible range is measured from
   const double zc = C.zerocut;
-  const double fr[2] = {F.frvol[c0], F.frvol[c0 + 1]};
-  const double pbar = fr[0] * F.cpp[c0] + fr[1] * F.cpp[c0 + 1];
-  const int4 nd = __ldg(F.ielnd + iel);
-  const int n[4] = {nd.x, nd.y, nd.z, nd.w};
-  double ub[4], vb[4];
-#pragma unroll
-  for (int j = 0; j < 4; j++) {
-    ub[j] = F.ndubar[n[j]];
-    vb[j] = F.ndvbar[n[j]];
-  }
-  // the plain closure's step (k_lag_state's component update): the
-  // fallback, and the state the admissible range is measured from
-  double pe[2], pv[2], pr[2], pp[2], pc[2];
-  for (int k = 0; k < 2; k++) {
-    const int icp = c0 + k;
+  const int icp = c0 + k;
+  double fr[2] = {0.0, 0.0}, pbar = 0.0;
+  double pe = 0.0, pv = 0.0, pr = 0.0, pp = 0.0, pc = 0.0;
+  if (cell) {
+    fr[0] = F.frvol[c0];
+    fr[1] = F.frvol[c0 + 1];
+    pbar = fr[0] * F.cpp[c0] + fr[1] * F.cpp[c0 + 1];
+    const double frk = k ? fr[1] : fr[0];
+    const int4 nd = __ldg(F.ielnd + iel);
+    const int n[4] = {nd.x, nd.y, nd.z, nd.w};
     const d4 a = F.cpfx[icp], b = F.cpfy[icp];
     const double cfx[4] = {a.x, a.y, a.z, a.w}, cfy[4] = {b.x, b.y, b.z, b.w};
     double cu[4], cv[4];
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-      cu[j] = fr[k] * ub[j];
-      cv[j] = fr[k] * vb[j];
+      cu[j] = frk * F.ndubar[n[j]];
+      cv[j] = frk * F.ndvbar[n[j]];
     }
     const double cpm = F.cpm[icp];
-    pe[k] = energy_update(F.cpe[icp], cpm, zc, dt, cfx, cfy, cu, cv);
-    pv[k] = V1 * fr[k];
-    pr[k] = DIV(cpm, pv[k]);
-    eos_pc(C, __ldg(F.icpmat + icp), pr[k], pe[k], pp[k], pc[k]);
+    pe = energy_update(F.cpe[icp], cpm, zc, dt, cfx, cfy, cu, cv);
+    pv = V1 * frk;
+    pr = DIV(cpm, pv);
+    eos_pc(C, __ldg(F.icpmat + icp), pr, pe, pp, pc);
   }
-  const double xeq = DIV((pp[0] - pp[1]) * V1,
-                         V0 * (DIV(pr[0] * pc[0], fr[0]) + DIV(pr[1] * pc[1], fr[1])));
+  // the other material's, from the partner lane
+  const double opp = __shfl_xor_sync(0xffffffffu, pp, 16);
+  const double opr = __shfl_xor_sync(0xffffffffu, pr, 16);
+  const double opc = __shfl_xor_sync(0xffffffffu, pc, 16);
+  if (!cell) return;
+  const double P0 = k ? opp : pp, P1 = k ? pp : opp;
+  const double R0 = k ? opr : pr, R1 = k ? pr : opr;
+  const double Q0 = k ? opc : pc, Q1 = k ? pc : opc;
+  const double xeq = DIV((P0 - P1) * V1, V0 * (DIV(R0 * Q0, fr[0]) + DIV(R1 * Q1, fr[1])));
   const double lo = fmin(0.0, xeq), hi = fmax(0.0, xeq), m = absF(xeq);
-  const float o1 = s.y[lane][0], o2 = s.y[lane][1];
+  const float o1 = s.y[lane & 15][0], o2 = s.y[lane & 15][1];
   const double xp = 0.5 * __ldg(F.mlp_norm + 2 * mlp::NI) * ((double)o1 - (double)o2);
   const double xm = fmin(fmax(xp, lo), hi);
-  const double x[2] = {xm, -xm};
-  bool ok = isfinite(o1) && isfinite(o2) && isfinite(xeq) &&
-            fabsf(o1 + o2) <= __ldg(F.mlp_norm + 2 * mlp::NI + 1) && xp >= lo - m && xp <= hi + m;
-#pragma unroll
-  for (int k = 0; k < 2; k++) ok = ok && pv[k] + x[k] * V0 > 0.0;
-  atomicAdd(F.mlp_count, 1ull);
-  if (!ok) atomicAdd(F.mlp_count + 1, 1ull);
-  for (int k = 0; k < 2; k++) {
-    const int icp = c0 + k;
-    double cpv = pv[k], cpe = pe[k], cpr = pr[k], cpp = pp[k], cpc = pc[k];
-    if (ok) {
-      const double cpm = F.cpm[icp];
-      cpv = pv[k] + x[k] * V0;
-      if (F.closure == 1) cpe = pe[k] - DIV(pbar * (x[k] * V0), maxF(cpm, zc));
-      cpr = DIV(cpm, cpv);
-      eos_pc(C, __ldg(F.icpmat + icp), cpr, cpe, cpp, cpc);
-      F.frvol[icp] = DIV(cpv, V1);
-    }
-    F.cpe[icp] = cpe;
-    F.cpvol[icp] = cpv;
-    F.cprho[icp] = cpr;
-    F.cpp[icp] = cpp;
-    F.cpcs2[icp] = cpc;
+  const double xk = k ? -xm : xm;  // this lane's material's share of the exchange
+  const bool ok = isfinite(o1) && isfinite(o2) && isfinite(xeq) &&
+                  fabsf(o1 + o2) <= __ldg(F.mlp_norm + 2 * mlp::NI + 1) && xp >= lo - m &&
+                  xp <= hi + m && V1 * fr[0] + xm * V0 > 0.0 && V1 * fr[1] + (-xm) * V0 > 0.0;
+  if (k == 0) {
+    atomicAdd(F.mlp_count, 1ull);
+    if (!ok) atomicAdd(F.mlp_count + 1, 1ull);
   }
+  double cpv = pv, cpe = pe, cpr = pr, cpp = pp, cpc = pc;
+  if (ok) {
+    const double cpm = F.cpm[icp];
+    cpv = pv + xk * V0;
+    if (F.closure == 1) cpe = pe - DIV(pbar * (xk * V0), maxF(cpm, zc));
+    cpr = DIV(cpm, cpv);
+    eos_pc(C, __ldg(F.icpmat + icp), cpr, cpe, cpp, cpc);
+    F.frvol[icp] = DIV(cpv, V1);
+  }
+  F.cpe[icp] = cpe;
+  F.cpvol[icp] = cpv;
+  F.cprho[icp] = cpr;
+  F.cpp[icp] = cpp;
+  F.cpcs2[icp] = cpc;
 }
 
 // ================================================================ launchers
