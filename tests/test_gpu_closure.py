@@ -197,3 +197,67 @@ def test_volume_only_closure_keeps_the_plain_flow_and_still_gains(trained):
     # the smaller gain of the two modes, and the one that varies more from
     # one trained network to the next
     assert fv < 0.9 * fp and r1v < 0.9 * r1p and r2v < 0.9 * r2p, ((fp, r1p, r2p), (fv, r1v, r2v))
+
+
+@pytest.mark.parametrize("mode", [1, 2], ids=["exchange", "volume_only"])
+def test_one_closure_step_matches_the_cpu_restatement(mode):
+    """k_mix_closure against oracle/closure.py: the exact build and the
+    oracle reach the same state after 30 plain steps (bit for bit), then one
+    step with the closure on each.  Element and node fields stay equal bit
+    for bit; the cells the closure hands back hold the plain step's values
+    bit for bit; the accepted cells agree to the precision of the network's
+    FP32 sums (the oracle sums the same BF16-rounded products in FP64).  An
+    untrained network suffices: its exchanges are clamped to the admissible
+    range."""
+    from oracle import closure as oclosure
+    from oracle.oracle import Oracle
+    from bookleaf_f90_gb300.setup import ic as icmod
+    params = closure.init_params(5)
+    norm = np.concatenate([[0.5, 1, 0.5, 1, 0.5, 1.4, 1.5, 0, 0.1, 0.3],
+                           [3, 2, 3, 2, 3, 2, 2, 300, 5, 2], [1e-3, 10.0]]).astype(np.float32)
+    net = closure.ClosureNet(params)
+    base = _problem(TEST, 80, 8)
+    pg, pc = base.copy(), base.copy()
+    s = Solver(pg, fp_mode=abi.FP_EXACT)
+    o = Oracle(pc)
+    for _ in range(30):
+        assert s.step() == 0 and o.step(pc.timestep) == 0
+    s.sync_to_host(0)
+    assert not compare(pg, pc, exact=True)
+    f = pc.fields
+    nmx = pc.sizes.nmx
+    before = {"frvol": f[abi.FRVOLUME].copy(), "cprho": f[abi.CPDENSITY].copy(),
+              "cpp": f[abi.CPPRESSURE].copy(), "cpcs2": f[abi.CPCS2].copy(),
+              "vol0": f[abi.ELVOLUME][f[abi.IMXEL][:nmx] - 1].copy()}
+    s.set_closure(net, norm, volume_only=(mode == 2))
+    assert s.step() == 0
+    s.sync_to_host(0)
+    seen, rejected = s.closure_stats()
+    s.close()
+    net.close()
+    assert o.step(pc.timestep) == 0
+    plain = {fid: f[fid].copy() for fid in (abi.CPVOLUME, abi.CPENERGY, abi.CPDENSITY,
+                                            abi.CPPRESSURE, abi.CPCS2, abi.FRVOLUME)}
+    ok = oclosure.apply(f, before, pc.timestep.dt, params, norm, mode,
+                        lambda m, r, e: icmod.eos(pc.config, m, r, e), pc.config.zerocut)
+    assert seen == nmx and rejected == int(np.sum(~ok)) and np.sum(ok) > 0
+    assert _same_state_outside_components(pg, pc)
+    c0 = f[abi.IMXFCP][:nmx] - 1
+    moved = 0
+    for fid in plain:
+        for k in (0, 1):
+            icp = c0 + k
+            g, c = pg.fields[fid][icp], f[fid][icp]
+            assert np.array_equal(g[~ok], c[~ok]), abi.NAMES[fid]
+            assert np.allclose(g[ok], c[ok], rtol=1e-7, atol=0), (abi.NAMES[fid], np.max(
+                np.abs(g[ok] - c[ok]) / np.abs(c[ok])))
+            moved += int(np.sum(g[ok] != plain[fid][icp][ok]))
+    assert moved > 0
+
+
+def _same_state_outside_components(pg, pc):
+    for fid in (abi.ELDENSITY, abi.ELENERGY, abi.ELPRESSURE, abi.ELVOLUME, abi.NDX, abi.NDY,
+                abi.NDU, abi.NDV, abi.CNMASS, abi.ELCS2):
+        if not np.array_equal(pg.fields[fid], pc.fields[fid]):
+            return False
+    return True
