@@ -78,3 +78,48 @@ def test_standardisation_and_exchange():
     assert np.allclose(x[:, :9].std(axis=0), 1, atol=1e-4)
     assert np.all(x[:, 9] == 0) and norm[19] == 1.0       # a constant feature
     assert np.allclose(t * norm[20], np.stack([x1, -x1], axis=1), rtol=1e-5, atol=1e-12)
+
+
+def test_closure_step_restatement_conserves_volume_and_energy(oracle_lib):
+    """One closure step on the CPU (oracle/closure.py) after 30 oracle steps:
+    each accepted cell's material volumes still add up to the cell's, the
+    fractions to 1, the energy moved between its materials sums to zero
+    (exchange mode) or no energy moves (volume only), and masses stay."""
+    from oracle import closure as oclosure
+    from oracle.oracle import Oracle
+    from bookleaf_f90_gb300.setup import ic as icmod
+    deck, frac = configs.sod_interface(80, 8, time_end=0.2, amplitude=0.0, periods=0, tilt=0.2,
+                                       rho_right=0.5, p_right=0.5)
+    p = Problem.from_deck(deck, material_fraction=frac)
+    o = Oracle(p)
+    for _ in range(30):
+        assert o.step(p.timestep) == 0
+    f = p.fields
+    nmx = p.sizes.nmx
+    el = f[abi.IMXEL][:nmx] - 1
+    c0 = f[abi.IMXFCP][:nmx] - 1
+    before = {"frvol": f[abi.FRVOLUME].copy(), "cprho": f[abi.CPDENSITY].copy(),
+              "cpp": f[abi.CPPRESSURE].copy(), "cpcs2": f[abi.CPCS2].copy(),
+              "vol0": f[abi.ELVOLUME][el].copy()}
+    assert o.step(p.timestep) == 0
+    params = closure.init_params(5)
+    norm = np.concatenate([[0.5, 1, 0.5, 1, 0.5, 1.4, 1.5, 0, 0.1, 0.3],
+                           [3, 2, 3, 2, 3, 2, 2, 300, 5, 2], [1e-3, 10.0]]).astype(np.float32)
+    energy = lambda g: g[abi.CPMASS][c0] * g[abi.CPENERGY][c0] + \
+        g[abi.CPMASS][c0 + 1] * g[abi.CPENERGY][c0 + 1]
+    for mode in (1, 2):
+        g = {k: v.copy() for k, v in f.items()}
+        ok = oclosure.apply(g, before, p.timestep.dt, params, norm, mode,
+                            lambda m, r, e: icmod.eos(p.config, m, r, e), p.config.zerocut)
+        assert ok.sum() > 0
+        V1 = g[abi.ELVOLUME][el]
+        assert np.allclose(g[abi.CPVOLUME][c0] + g[abi.CPVOLUME][c0 + 1], V1, rtol=1e-13, atol=0)
+        assert np.allclose(g[abi.FRVOLUME][c0] + g[abi.FRVOLUME][c0 + 1], 1.0, rtol=0, atol=1e-13)
+        assert np.allclose(energy(g), energy(f), rtol=1e-12, atol=0)
+        moved = g[abi.CPVOLUME][c0] != f[abi.CPVOLUME][c0]
+        assert np.array_equal(moved, ok) or moved[ok].any()
+        if mode == 2:
+            assert np.array_equal(g[abi.CPENERGY], f[abi.CPENERGY])
+        else:
+            assert not np.array_equal(g[abi.CPENERGY], f[abi.CPENERGY])
+        assert np.array_equal(g[abi.CPMASS], f[abi.CPMASS])
