@@ -123,3 +123,30 @@ def test_closure_step_restatement_conserves_volume_and_energy(oracle_lib):
         else:
             assert not np.array_equal(g[abi.CPENERGY], f[abi.CPENERGY])
         assert np.array_equal(g[abi.CPMASS], f[abi.CPMASS])
+
+
+def test_interface_and_error_measures():
+    """The measures the closure is judged by: a run against itself is at
+    zero distance; moving volume between the materials of one mixed cell
+    shifts that row's interface by the moved volume over the row's height
+    and shows up in the material errors against the unmoved state."""
+    nx, ny = 40, 4
+    a = _problem(nx, ny)
+    b = a.copy()
+    idx = closure.grid_index(a, nx, ny)
+    assert closure.against_plain(a, a, idx, nx, ny) == (0.0, 0.0, 0.0)
+    f = b.fields
+    c0 = f[abi.IMXFCP][0] - 1                # the first mixed cell's components
+    dv = 0.1 * min(f[abi.CPVOLUME][c0], f[abi.CPVOLUME][c0 + 1])
+    f[abi.CPVOLUME][c0] += dv
+    f[abi.CPVOLUME][c0 + 1] -= dv
+    shift, l1_mixed, l1_all = closure.against_plain(b, a, idx, nx, ny)
+    row_height = 0.1 / ny
+    dx = 1.0 / nx
+    assert abs(shift - dv / row_height / dx) < 1e-9 * shift
+    assert l1_mixed == 0.0 and l1_all == 0.0     # cell densities unchanged
+    V, M, _ = closure.material_sums(a, idx, nx * ny)
+    cells = idx[f[abi.IMXEL][:a.sizes.nmx] - 1]
+    fe, r1, r2 = closure.mixed_errors(b, idx, (V, M), cells)
+    assert fe > 0 and r1 > 0 and r2 > 0
+    assert closure.mixed_errors(a, idx, (V, M), cells) == (0.0, 0.0, 0.0)
