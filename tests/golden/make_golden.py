@@ -26,15 +26,13 @@ CASES = {
 
 
 def _bits(a):
-    """Order-dependent exact checksum of a float64 array."""
+    """Exact checksum of a float64 array: the first 16 hex digits of the
+    SHA-256 of its little-endian bytes in order, so any change of any bit
+    of any element, or of the elements' order, changes it."""
+    import hashlib
     import numpy as np
-    v = np.ascontiguousarray(a, dtype=np.float64).view(np.uint64)
-    h = np.uint64(1469598103934665603)
-    acc = 0
-    for chunk in np.array_split(v, max(1, v.size // 4096)):
-        acc = (acc * 1000003 + int(np.bitwise_xor.reduce(chunk * np.uint64(0x9E3779B97F4A7C15))
-                                   if chunk.size else 0)) % (1 << 61)
-    return "%016x" % ((acc ^ int(h)) & ((1 << 64) - 1))
+    v = np.ascontiguousarray(a, dtype="<f8")
+    return hashlib.sha256(v.tobytes()).hexdigest()[:16]
 
 
 def summarise(p):

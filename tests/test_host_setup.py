@@ -14,8 +14,9 @@ import pytest
 from bookleaf_f90_gb300 import Problem, abi, configs
 from bookleaf_f90_gb300 import build as blbuild
 
+import golden
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_INPUT = "/root/reference/input"
 
 HG = configs.sedov(16).replace("cvisc2=0.75\n", "cvisc2=0.75\n kappaall=0.05\n pmeritall=0.3\n")
 DTNOT = configs.sod(24, 4).replace(
@@ -95,13 +96,10 @@ def test_cpp_setup_matches_python(exe, tmp_path, name):
     check_same(Problem.from_deck(deck), run_dump(exe, deck, tmp_path, name))
 
 
-@pytest.mark.parametrize("name", ["sod_sm_lag_small", "sod_mm_lag_small", "sedov_lag_small",
-                                  "sedov_eul_small", "blast_sm_eul_small", "sod_sm_eul_small"])
+@pytest.mark.parametrize("name", golden.deck_names())
 def test_cpp_setup_matches_python_on_reference_decks(exe, tmp_path, name):
-    path = os.path.join(REF_INPUT, name)
-    if not os.path.exists(path):
-        pytest.skip("reference decks not present on this machine")
-    deck = open(path).read()
+    """Every control file of the reference (tests/golden/decks)."""
+    deck = golden.deck_text(name)
     try:
         p = Problem.from_deck(deck)
     except ValueError as e:  # a deck the harness does not support
