@@ -47,13 +47,20 @@ sys.path.insert(0, HERE)
 B_LAG = 724
 B_EUL = 1628
 B_GETDT = 164
-# From the ncu capture of k_getdt at the end-of-run state (t = 1) of the
-# default workload: the FP64-pipe instructions (DFMA+DMUL+DADD+DSETP) it
-# executes per zone, which with the FMA rate measured live below place
-# k_getdt against the FP64 issue roof that binds it, and its DRAM traffic
-# per launch (dram__bytes_read + _write).
-FP64_PER_ZONE_GETDT = 226.9
-TRAFFIC_GETDT_BYTES = 50.9e6
+# the headline metric, printed by both arms
+METRIC = "zone-cycles/s FP64 (1 GB300, %HBM roof); batched+MLP vs plain GPU at stated L1 err"
+
+
+def load_profile(name="k_getdt_current.json"):
+    """The committed summary of the latest single-kernel ncu capture of
+    k_getdt (profiles/k_getdt_current.json): its FP64-pipe thread
+    instructions per zone and DRAM bytes per launch, with the command and
+    mesh size they were taken at; None where absent."""
+    path = os.path.join(HERE, "profiles", name)
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        return json.load(f)
 
 
 def workload_deck(name, size):
@@ -91,84 +98,150 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
+_NVML_REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+                 0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+
+class _Nvml:
+    """Read-only NVML queries through ctypes (the driver's libnvidia-ml):
+    SM clock, its maximum and the active clock-event reasons of one GPU."""
+
+    def __init__(self, torch_index):
+        import ctypes as ct
+        self.ct = ct
+        self.lib = ct.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.dev = ct.c_void_p()
+        rc = -1
+        try:
+            import torch
+            uuid = str(torch.cuda.get_device_properties(torch_index).uuid)
+            uuid = uuid if uuid.startswith("GPU-") else "GPU-" + uuid
+            rc = self.lib.nvmlDeviceGetHandleByUUID(uuid.encode(), ct.byref(self.dev))
+        except Exception:
+            rc = -1
+        if rc != 0:
+            rc = self.lib.nvmlDeviceGetHandleByIndex_v2(ct.c_uint(torch_index), ct.byref(self.dev))
+        if rc != 0:
+            raise OSError("no NVML handle")
+        self.reasons_fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+
+    def sample(self):
+        ct = self.ct
+        clk, mx, rs = ct.c_uint(0), ct.c_uint(0), ct.c_ulonglong(0)
+        self.lib.nvmlDeviceGetClockInfo(self.dev, 1, ct.byref(clk))       # NVML_CLOCK_SM
+        self.lib.nvmlDeviceGetMaxClockInfo(self.dev, 1, ct.byref(mx))
+        self.reasons_fn(self.dev, ct.byref(rs))
+        return clk.value, mx.value, rs.value
+
+
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons during the timed region."""
+    """SM clock and clock-event reasons DURING the timed region: a thread
+    polls NVML every 0.5 ms between __enter__ and __exit__ (the library's
+    calls release the interpreter lock), so that even a region of a few
+    milliseconds gets samples; one sample is also taken at each end.  Falls
+    back to one nvidia-smi query at each end where NVML cannot be loaded."""
 
     def __init__(self, gpu_index):
         self.idx = gpu_index
         self.samples = []
-        self.proc = None
+        self.how = "nvml poll 0.5 ms"
+        try:
+            self.nv = _Nvml(gpu_index)
+        except (OSError, AttributeError):
+            self.nv = None
+            self.how = "nvidia-smi at both ends"
+
+    def _smi(self):
+        try:
+            out = subprocess.run(
+                ["nvidia-smi", "-i", str(self.idx), "--query-gpu=clocks.sm,clocks.max.sm,"
+                 "clocks_event_reasons.active", "--format=csv,noheader,nounits"],
+                capture_output=True, text=True, timeout=10).stdout.strip().split(",")
+            self.samples.append((float(out[0]), float(out[1]), int(out[2].strip(), 16)))
+        except Exception:
+            pass
+
+    def _poll(self):
+        while not self.stop.is_set():
+            self.samples.append(self.nv.sample())
+            time.sleep(0.0005)
 
     def __enter__(self):
-        try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.idx), "--query-gpu=clocks.sm,clocks.max.sm,"
-                 "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
-                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "100"],
-                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
-            self.t.start()
-        except (OSError, FileNotFoundError):
-            self.proc = None
+        self.stop = threading.Event()
+        if self.nv is None:
+            self._smi()
+            return self
+        self.samples.append(self.nv.sample())
+        self.t = threading.Thread(target=self._poll, daemon=True)
+        self.t.start()
         return self
 
-    def _read(self):
-        for line in self.proc.stdout:
-            self.samples.append([x.strip() for x in line.split(",")])
-
     def __exit__(self, *a):
-        if self.proc:
-            self.proc.terminate()
-            try:
-                self.proc.wait(timeout=5)
-            except subprocess.TimeoutExpired:
-                self.proc.kill()
+        if self.nv is None:
+            self._smi()
+            return
+        self.stop.set()
+        self.t.join()
+        self.samples.append(self.nv.sample())
 
     def summary(self):
         if not self.samples:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = sorted(float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit())
-        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        sm = sorted(s[0] for s in self.samples)
         reasons = set()
         for s in self.samples:
-            for i, n in enumerate(names):
-                if len(s) > 3 + i and s[3 + i].lower() == "active":
-                    reasons.add(n)
-        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(self.samples)}
+            for bit, name in _NVML_REASONS.items():
+                if s[2] & bit:
+                    reasons.add(name)
+        return {"sm_mhz": sm[len(sm) // 2], "sm_min_mhz": sm[0],
+                "sm_max_mhz": max(s[1] for s in self.samples),
+                "reasons": sorted(reasons), "samples": len(self.samples), "how": self.how}
 
 
-def cpu_sample(deck, steps):
-    """The CPU restatement advancing `steps` steps of the workload; returns
-    (zone-cycles/s, seconds).  Runs in a worker process."""
+def cpu_sample(deck, steps, warmup=1):
+    """The CPU restatement advancing `steps` steps of the workload from
+    t = 0, after `warmup` untimed steps on a copy of the same initial state;
+    returns (zone-cycles/s, seconds).  Runs in a spawned worker process."""
     sys.path.insert(0, HERE)
     from bookleaf_f90_gb300 import Problem
     from oracle.oracle import Oracle
     p = Problem.from_deck(deck)
+    if warmup > 0:
+        q = p.copy()
+        oq = Oracle(q)
+        for _ in range(warmup):
+            if oq.step(q.timestep) != 0:
+                break
+        del oq, q
     o = Oracle(p)
-    o.step(p.timestep)   # warm-up step (first step uses dt_initial)
     t0 = time.perf_counter()
+    n = 0
     for _ in range(steps):
         if o.step(p.timestep) != 0:
             break
+        n += 1
     t = time.perf_counter() - t0
-    return p.nel * steps / t, t
+    return p.nel * n / t, t
 
 
-def cpu_baseline(deck, nel, target_s=12.0, cores=1):
-    """Bounded sample of the workload on the host's cores (spawned workers)."""
+def cpu_baseline(deck, nel, target_s=12.0, cores=1, steps=0, warmup=1):
+    """The workload on the host's cores (spawned workers, one independent
+    replica each): `steps` steps from t = 0, or with steps = 0 as many as
+    fill about target_s seconds (calibrated on one step).  Returns (summed
+    zone-cycles/s, steps, slowest worker's seconds)."""
     import multiprocessing as mp
     from oracle import oracle as orc
     orc.build()
-    # calibrate one step
     ctx = mp.get_context("spawn")
-    with ctx.Pool(1) as pool:
-        rate, t = pool.apply(cpu_sample, (deck, 1))
-    steps = max(2, int(target_s * rate / nel))
+    if steps <= 0:
+        with ctx.Pool(1) as pool:
+            rate, t = pool.apply(cpu_sample, (deck, 1, 0))
+        steps = max(2, int(target_s * rate / nel))
     with ctx.Pool(cores) as pool:
-        res = pool.starmap(cpu_sample, [(deck, steps)] * cores)
+        res = pool.starmap(cpu_sample, [(deck, steps, warmup)] * cores)
     rate = sum(r for r, _ in res)
     return rate, steps, max(t for _, t in res)
 
@@ -262,8 +335,7 @@ def run_ensemble(args, torch):
     plain = zc_p / (ms_p * 1e-3)
     hbm_peak, peak_kind = load_peaks()
     achieved = value * B_EUL / 1e9
-    return {"metric": "zone-cycles/s FP64 (1 GB300, %HBM roof); batched ensemble vs plain "
-                      "per-mesh GPU path",
+    return {"metric": METRIC, "what": "batched ensemble vs the plain per-mesh GPU path",
             "value": value, "unit": "zone-cycles/s", "n_gpus": 1, "steps": nsteps,
             "warmup": W, "ms_per_step": ms_b / max(1, nsteps), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -432,8 +504,7 @@ def run_closure(args, torch):
     value = rl["rate"]
     achieved = value * B_LAG / 1e9
     names = ("vol_fraction_abs", "rho1_rel", "rho2_rel")
-    return {"metric": "zone-cycles/s FP64 (1 GB300); two-material Sod with the learned "
-                      "mixed-cell closure",
+    return {"metric": METRIC, "what": "two-material Sod with the learned mixed-cell closure",
             "value": value, "unit": "zone-cycles/s", "n_gpus": 1, "steps": rl["steps"],
             "warmup": W, "ms_per_step": rl["ms"] / max(1, rl["steps"]),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -612,8 +683,8 @@ def run_closure_ensemble(args, torch):
     plain_alone = zc_p / (ms_p * 1e-3)
     hbm_peak, peak_kind = load_peaks()
     achieved = value * B_LAG / 1e9
-    return {"metric": "zone-cycles/s FP64 (1 GB300); batched two-material tubes with the "
-                      "learned closure vs the plain per-mesh GPU path",
+    return {"metric": METRIC, "what": "batched two-material tubes with the learned closure "
+                                      "vs the plain per-mesh GPU path",
             "value": value, "unit": "zone-cycles/s", "n_gpus": 1, "steps": nsteps,
             "warmup": W, "ms_per_step": ms_b / max(1, nsteps), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -684,16 +755,26 @@ def main():
         from bookleaf_f90_gb300 import Problem
         nel = Problem.from_deck(deck).nel
         cores = os.cpu_count() or 1
-        rate, steps, t = cpu_baseline(deck, nel, target_s=20.0, cores=cores)
-        line = {"impl": "reference", "metric": "zone-cycles/s FP64", "value": rate,
+        # --steps K: the same K steps from t = 0 as the GPU arm, unless
+        # that would take more than about 150 s of CPU time per core (at the
+        # restatement's ~3M zone-cycles/s on one core); --steps 0: a
+        # sample of about 20 s per core
+        req = args.steps
+        steps = min(req, max(2, int(150.0 * 3.0e6 / nel))) if req > 0 else 0
+        rate, steps, t = cpu_baseline(deck, nel, target_s=20.0, cores=cores, steps=steps,
+                                      warmup=min(args.warmup, 1))
+        line = {"impl": "reference", "metric": METRIC, "value": rate,
                 "unit": "zone-cycles/s", "n_gpus": args.gpus, "steps": steps,
                 "warmup": args.warmup, "higher_is_better": True, "dtype": "f64",
                 "data": "synthetic", "config": {"workload": wname, "nel": nel},
                 "cpu_baseline": {"value": rate, "unit": "zone-cycles/s", "cores": cores,
                                  "kind": "port",
-                                 "sample": "%d steps of %s on each of %d cores (independent "
-                                           "replicas of the serial CPU restatement), %.1f s"
-                                           % (steps, wname, cores, t)},
+                                 "sample": "the first %d steps of %s from t = 0 on each of %d "
+                                           "cores (independent replicas of the serial CPU "
+                                           "restatement, -O2 -ffp-contract=off), slowest %.1f s%s"
+                                           % (steps, wname, cores, t,
+                                              "" if req <= 0 or steps == req else
+                                              "; %d requested, capped to bound the run" % req)},
                 "e2e": {"value": rate, "unit": "zone-cycles/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
@@ -774,9 +855,14 @@ def main():
     lag_ms = kms[1] + kms[2] + kms[3]
     hbm_peak, peak_kind = load_peaks()
     achieved = B_GETDT * nel / (k_ms * 1e-3) / 1e9
+    prof = load_profile()
+    traffic = (prof["dram_bytes_per_launch"] * nel / prof["nel"]) if prof else None
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-            "frac": achieved / hbm_peak, "traffic": TRAFFIC_GETDT_BYTES * nel / 262144,
-            "traffic_unit": "bytes per launch (ncu capture at 512x512, scaled by zones)",
+            "frac": achieved / hbm_peak, "traffic": traffic,
+            "traffic_unit": "bytes per launch, from profiles/k_getdt_current.json (ncu, "
+                            "dram__bytes_read.sum + dram__bytes_write.sum%s)"
+                            % ("" if not prof or prof["nel"] == nel else
+                               ", scaled from %d zones" % prof["nel"]),
             "kernel": "k_getdt",
             "peak_kind": peak_kind, "kernel_ms": k_ms,
             "note": "the FP64 issue rate, not HBM, bounds this path; see fp64",
@@ -788,11 +874,16 @@ def main():
     step_bytes = bytes_zc * nel
     from bookleaf_f90_gb300 import _lib
     rates = _lib.fp64_rates()
-    fp64_ach = FP64_PER_ZONE_GETDT * nel / (k_ms * 1e-3) / 1e9
+    ipz = prof["fp64_pipe_instr_per_zone"] if prof else None
+    fp64_ach = ipz * nel / (k_ms * 1e-3) / 1e9 if ipz else None
     fp64 = {"bound": "fp64", "kernel": "k_getdt", "unit": "G FP64-pipe instr/s",
-            "achieved": fp64_ach, "peak": rates["dfma"], "frac": fp64_ach / rates["dfma"],
+            "achieved": fp64_ach, "peak": rates["dfma"],
+            "frac": fp64_ach / rates["dfma"] if ipz else None,
             "peak_kind": "measured live (DFMA issue loop, bl_fp64_rates)",
-            "instr_per_zone": FP64_PER_ZONE_GETDT, "rates_gops": rates,
+            "instr_per_zone": ipz,
+            "instr_source": "profiles/k_getdt_current.json: %s" % (
+                prof["how"] if prof else "absent"),
+            "rates_gops": rates,
             "step_ms": t_max / max(1, nsteps),
             "hbm_frac_whole_step": (step_bytes * nsteps / (t_max * 1e-3) / 1e9) / hbm_peak}
     s.close()
@@ -828,8 +919,13 @@ def main():
         e2e = {"value": e2e_val, "unit": "zone-cycles/s",
                "h2d_bytes_per_step": int(h2d / n_e) + 2 * 64,
                "d2h_bytes_per_step": int(d2h / n_e) + 3 * 64,
-               "note": "bl_init upload + %d per-call steps (getdt, lagstep%s) + full state "
-                       "download, host pinned" % (n_e, ", alestep" if eul else "")}
+               "note": "bl_init upload of every registered host array + %d per-call steps "
+                       "(getdt, lagstep%s; each call uploads the 64-byte step header when the "
+                       "host changed it and downloads it) + full state download, host pinned. "
+                       "The state stays resident between calls as the reference's dataAPI "
+                       "arrays do, so the per-step byte counts are the init upload and the "
+                       "final download divided by the %d steps plus the headers"
+                       % (n_e, ", alestep" if eul else "", n_e)}
         se.close()
 
     cpu = None
@@ -840,7 +936,7 @@ def main():
                          "restatement, -O2 -ffp-contract=off), %.1f s" % (steps, wname, t)}
 
     if rank == 0:
-        line = {"metric": "zone-cycles/s FP64 (1 GB300, %HBM roof)", "value": value,
+        line = {"metric": METRIC, "value": value,
                 "unit": "zone-cycles/s", "n_gpus": world, "steps": nsteps,
                 "warmup": args.warmup, "ms_per_step": t_max / max(1, nsteps),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

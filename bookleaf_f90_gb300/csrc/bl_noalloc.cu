@@ -1,8 +1,8 @@
 // bl_noalloc.cu -- bl_getdt_noalloc: the getdt step without any allocation.
 //
 // Some callers cannot call cudaMalloc: a host that hands out every byte of
-// device memory from its own pool, or code that must not allocate in the
-// middle of recorded work.  For them this entry point runs the computation
+// device memory from its own pool, where an allocation behind its back
+// would fail or break its accounting.  For them this entry point runs the computation
 // of bl_getdt (k_getdt: edge viscosity, elcs2+elvisc, CFL and divergence
 // limits, dt selection) on device arrays the caller passes, in the
 // reference's own layout, without a bl_ctx.  The only device memory it
@@ -232,7 +232,8 @@ __global__ void __launch_bounds__(kBS) k_getdt_noalloc(NaParams P, unsigned char
     }
     const double cs2v = A.elcs2[iel] + visc;
     A.elcs2_out[iel] = cs2v;
-    const int ireg = A.ielreg[iel] - 1;
+    int ireg = A.ielreg[iel] - 1;
+    if (ireg < 0 || ireg >= BL_MAXREG) ireg = 0;  // out-of-range regions read region 1
     double r11;
     if (P.zdtnotreg[ireg]) {
       r11 = DBL_MAX;

@@ -379,19 +379,23 @@ typedef struct {
 
 /* No counterpart in the reference: an allocation-free variant of bl_getdt
  * for callers that cannot call cudaMalloc -- for example a host that hands
- * out all device memory from its own pool, or code running where a device
- * allocation would break a captured sequence of work.  It runs the same
- * computation as bl_getdt (edge viscosity, elcs2+elvisc, CFL and divergence
- * limits, time_dr_calc/time_dr_end) on arrays the caller passes, without a
- * bl_ctx.  Its reduction scratch is a fixed file-scope device array, held by
- * every GPU that loads the library until the process exits; nothing is
- * allocated or freed by this call.  The first call on a device looks up that
- * array's device address (cudaGetSymbolAddress); make that first call
- * before any stream capture.  Calls that overlap on the GPU (other streams,
- * other host threads) share the array and race: serialise them.  Returns
- * the reference's error codes like bl_getdt; nel > BL_NOALLOC_MAX_NEL is
- * rejected with FAILURE.  stream is a cudaStream_t (NULL: the legacy
- * default stream); the call waits for it before returning timestep. */
+ * out every byte of device memory from its own pool, so that a library
+ * allocating behind its back would fail or break its accounting.  It runs
+ * the same computation as bl_getdt (edge viscosity, elcs2+elvisc, CFL and
+ * divergence limits, time_dr_calc/time_dr_end) on arrays the caller passes,
+ * without a bl_ctx.  Its reduction scratch is a fixed file-scope device
+ * array, held by every GPU that loads the library until the process exits;
+ * nothing is allocated or freed by this call.  The first call on a device
+ * looks up that array's device address (cudaGetSymbolAddress); make that
+ * first call before any stream capture.  Calls that overlap on the GPU
+ * (other streams, other host threads) share the array and race: serialise
+ * them.  elcs2_out must not alias elcs2 (neighbouring elements read elcs2
+ * while it is written), and every ielreg entry must lie in 1..BL_MAXREG
+ * (entries outside it read region 1's settings).
+ * Returns the reference's error codes like bl_getdt; nel >
+ * BL_NOALLOC_MAX_NEL is rejected with FAILURE.  stream is a cudaStream_t
+ * (NULL: the legacy default stream); the call copies the result record to
+ * the host and synchronises that stream before it returns timestep. */
 int bl_getdt_noalloc(const bl_getdt_arrays *arrays, const bl_config *config,
                      bl_timestep *timestep, void *stream, bl_error *error);
 
