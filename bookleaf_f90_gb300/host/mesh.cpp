@@ -6,13 +6,13 @@
 //                                                     lines, interior guess and
 //                                                     relaxation, corner BCs)
 //   setup_mesh_line         setup_mesh.F90:1750-1855
+//   setup_mesh_arc          setup_mesh.F90:1857-2062
 //   setup_mesh_transfer     setup_mesh.F90:1091-1250 (node/element numbering)
 //   utils_kn_getconn/getsconn/corrconn   utils_kn_connectivity.f90:30-170
 //   init_kn_nodetype        init_kn.f90:78-106
 //
-// One mesh region of type LIN1 or LIN2 whose four sides are single LINE
-// segments: every structured deck of the reference except the ARC-sided
-// ones.  Node l runs along region_dim(:,2), k along region_dim(:,1), as the
+// One mesh region of type LIN1 or LIN2 whose four sides are single LINE,
+// LINK, ARC_A or ARC_C segments: every deck of the reference.  Node l runs along region_dim(:,2), k along region_dim(:,1), as the
 // reference stores them, so node and element numbers match the reference's.
 #include <algorithm>
 #include <cmath>
@@ -112,6 +112,111 @@ void side_line(Grid& g, const double* point, int segbc, int ind, double zerocut,
         }
         if (done) break;
       }
+    }
+  }
+}
+
+constexpr double kPi = 3.1415926535897932385;
+constexpr double kTwoPi = 6.2831853071795864770;
+
+// polar angle of the offset (d along s, w along r) from an arc's centre as
+// setup_mesh_arc measures it: atan(d/w), moved by pi where w < 0 and by
+// 2 pi where only d < 0 (w near zero taken as zerocut)
+double arc_angle(double d, double w, double zerocut) {
+  const double den = std::fabs(w) < zerocut ? zerocut : w;
+  double th = std::atan(d / den);
+  if (den < 0.0) th = th + kPi;
+  else if (d < 0.0) th = th + kTwoPi;
+  return th;
+}
+
+// setup_mesh_arc (setup_mesh.F90:1857-2062) for one side: points at equal
+// steps of polar angle about (s0, r0) = (point(6), point(5)) from the
+// segment's first point to its second, radius linear in the angle; ARC_A
+// runs anticlockwise, ARC_C is generated from its second point to its
+// first and then reversed.  With weights (point(7:8)) the angles are
+// relaxed first; that form is restated as written, including its use of
+// the relaxation's last residual as the start radius and of r0 as the s
+// offset.
+void side_arc(Grid& g, const double* point, int segbc, int sty, int ind, double zerocut,
+              double tol) {
+  const int no_l = g.no_l, no_k = g.no_k;
+  int l1, k1, l2, k2;
+  switch (ind) {
+    case 1: l1 = 1; k1 = 1; l2 = 1; k2 = no_k; break;
+    case 2: l1 = 1; k1 = no_k; l2 = no_l; k2 = no_k; break;
+    case 3: l1 = no_l; k1 = no_k; l2 = no_l; k2 = 1; break;
+    default: l1 = no_l; k1 = 1; l2 = 1; k2 = 1; break;
+  }
+  const bool fl = sty == 2;
+  const double s1 = fl ? point[2] : point[0], r1 = fl ? point[3] : point[1];
+  const double s2 = fl ? point[0] : point[2], r2 = fl ? point[1] : point[3];
+  const double r0 = point[4], s0 = point[5];
+  double w1 = point[6], w2 = point[7];
+  const int kmin = std::min(k1, k2), kmax = std::max(k1, k2);
+  const int lmin = std::min(l1, l2), lmax = std::max(l1, l2);
+  const double fac = w1 + w2;
+  bool weighted = false;
+  if (fac > zerocut) {
+    w1 = w1 / fac;
+    w2 = w2 / fac;
+    weighted = true;
+  }
+  const double dd = s1 - s0, w3 = r1 - r0;
+  const double theta1 = arc_angle(dd, w3, zerocut);
+  double d1 = s2 - s0;
+  const double w4 = r2 - r0;
+  double theta2 = arc_angle(d1, w4, zerocut);
+  if (theta2 > theta1) theta2 = theta2 - kTwoPi;
+  const double d2 = std::sqrt(w4 * w4 + d1 * d1);
+  d1 = std::sqrt(w3 * w3 + dd * dd);
+  const bool along_k = lmin == lmax;
+  const int lo = along_k ? kmin : lmin, hi = along_k ? kmax : lmax;
+  const int end2 = along_k ? k2 : l2;
+  auto R = [&](int i) -> double& { return along_k ? g.r(l1 - 1, i - 1) : g.r(i - 1, k1 - 1); };
+  auto S = [&](int i) -> double& { return along_k ? g.s(l1 - 1, i - 1) : g.s(i - 1, k1 - 1); };
+  auto B = [&](int i) -> int& { return along_k ? g.b(l1 - 1, i - 1) : g.b(i - 1, k1 - 1); };
+  const double nd = (double)(hi - lo);
+  const double dtheta = theta1 - theta2;
+  for (int ii = lo; ii <= hi; ii++) {
+    const int ij = lo == end2 ? hi + lo - ii : ii;
+    const double theta = theta1 - (double)(ii - lo) * dtheta / nd;
+    double dl = (d1 - d2) / dtheta;
+    dl = d1 + dl * (theta - theta1);
+    R(ij) = r0 + dl * std::cos(theta);
+    S(ij) = s0 + dl * std::sin(theta);
+    B(ij) = segbc;
+  }
+  g.r(l1 - 1, k1 - 1) = r1;
+  g.r(l2 - 1, k2 - 1) = r2;
+  g.s(l1 - 1, k1 - 1) = s1;
+  g.s(l2 - 1, k2 - 1) = s2;
+  if (weighted) {
+    for (int ii = lo; ii <= hi; ii++) {
+      const int ij = lo == end2 ? hi + lo - ii : ii;
+      R(ij) = theta1 - (double)(ii - lo) * dtheta / nd;
+    }
+    while (true) {
+      bool done = true;
+      for (int ii = lo + 1; ii < hi; ii++) {
+        d1 = w1 * R(ii - 1) + w2 * R(ii + 1) - R(ii);
+        if (std::fabs(d1) > tol) done = false;
+        R(ii) = R(ii) + d1;
+      }
+      if (done) break;
+    }
+    for (int ii = lo + 1; ii < hi; ii++) {
+      const double theta = R(ii);
+      double dl = (d1 - d2) / dtheta;
+      dl = d1 + dl * (theta - theta1);
+      R(ii) = r0 + dl * std::cos(theta);
+      S(ii) = r0 + dl * std::sin(theta);
+    }
+  }
+  if (fl) {
+    for (int jj = 0; jj <= (hi - lo) / 2; jj++) {
+      std::swap(R(lo + jj), R(hi - jj));
+      std::swap(S(lo + jj), S(hi - jj));
     }
   }
 }
@@ -237,11 +342,14 @@ MeshData generate_mesh(const Namelist* mesh_nl, double zerocut) {
     else if (st == "POINT") sty = 4;
     else if (st == "LINK") sty = 5;
     else throw DeckError("ERROR: unrecognised segment type");
-    if (sty != 1 && sty != 5) throw DeckError("ERROR: segment type " + st + " not supported");
+    if (sty == 4) throw DeckError("ERROR: side_type is POINT but DJN off");
     const int b = bc_code(segbc[iseg - 1].as_str());
     double point[8];
     for (int q = 0; q < 8; q++) point[q] = segpos[(size_t)(iseg - 1) * 8 + q].as_real();
-    side_line(g, point, b, ind, zerocut, tol, om, typ);
+    if (sty == 2 || sty == 3)
+      side_arc(g, point, b, sty, ind, zerocut, tol);
+    else
+      side_line(g, point, b, ind, zerocut, tol, om, typ);
   }
   // interior initial guess (setup_mesh.F90:713-752)
   const int l1 = 2, k1 = 2, l2 = no_l - 1, k2 = no_k - 1;

@@ -7,13 +7,14 @@ Host-side restatement of the reference's setup (out of the GPU hot path):
                                                     lines, interior guess and
                                                     relaxation, corner BCs)
   setup_mesh_line         setup_mesh.F90:1750-1855
+  setup_mesh_arc          setup_mesh.F90:1857-2062
   setup_mesh_transfer     setup_mesh.F90:1091-1250 (node/element numbering)
   utils_kn_getconn/getsconn/corrconn   utils_kn_connectivity.f90:30-170
   init_kn_nodetype        init_kn.f90:78-106
 
 Supported: one mesh region of type LIN1 or LIN2 whose four sides are single
-LINE segments -- every structured deck in the reference's input/ directory
-except the Noh decks' ARC segments.  Node ``l`` runs along region_dim(:,2),
+LINE, LINK, ARC_A or ARC_C segments -- every deck in the reference's
+input/ directory.  Node ``l`` runs along region_dim(:,2),
 ``k`` along region_dim(:,1), exactly as the reference stores them, so node and
 element numbers match the reference's.
 """
@@ -101,6 +102,110 @@ def _side_line(rr, ss, bc, seg, ind, no_l, no_k, zerocut, tol, om, rtyp):
                     break
 
 
+PI = 3.1415926535897932385
+TWOPI = 6.2831853071795864770
+
+
+def _arc_angle(d, w, zerocut):
+    """Polar angle of the offset (d along s, w along r) from the arc's
+    centre, in [0, 2 pi) as setup_mesh_arc measures it: atan(d / w) moved by
+    pi where w < 0 and by 2 pi where only d < 0 (w near zero taken as
+    zerocut)."""
+    import math
+    den = zerocut if abs(w) < zerocut else w
+    th = math.atan(d / den)
+    if den < 0.0:
+        th = th + PI
+    elif d < 0.0:
+        th = th + TWOPI
+    return th
+
+
+def _side_arc(rr, ss, bc, seg, ind, no_l, no_k, zerocut, tol, om):
+    """setup_mesh_arc (setup_mesh.F90:1857-2062) for one side: points at
+    equal steps of polar angle about (s0, r0) = (point(6), point(5)) from
+    the segment's first point to its second, with the radius interpolated
+    linearly in the angle; ARC_A runs anticlockwise, ARC_C is generated
+    from its second point to its first and then reversed.  With weights
+    (point(7:8)) the angles are relaxed first.  Restated as written,
+    including two quirks of the weighted form: the radius slope there uses
+    the relaxation's last residual in place of the start radius, and the
+    s coordinate is offset by r0."""
+    import math
+    l1, k1, l2, k2 = {1: (1, 1, 1, no_k), 2: (1, no_k, no_l, no_k),
+                      3: (no_l, no_k, no_l, 1), 4: (no_l, 1, 1, 1)}[ind]
+    p = seg["point"]
+    fl = seg["typ"] == 2
+    if fl:
+        s1, r1, s2, r2 = p[2], p[3], p[0], p[1]
+    else:
+        s1, r1, s2, r2 = p[0], p[1], p[2], p[3]
+    r0, s0, w1, w2 = p[4], p[5], p[6], p[7]
+    kmin, kmax = min(k1, k2), max(k1, k2)
+    lmin, lmax = min(l1, l2), max(l1, l2)
+    fac = w1 + w2
+    weighted = False
+    if fac > zerocut:
+        w1 = w1 / fac
+        w2 = w2 / fac
+        weighted = True
+    dd = s1 - s0
+    w3 = r1 - r0
+    theta1 = _arc_angle(dd, w3, zerocut)
+    d1 = s2 - s0
+    w4 = r2 - r0
+    theta2 = _arc_angle(d1, w4, zerocut)
+    if theta2 > theta1:
+        theta2 = theta2 - TWOPI
+    d2 = math.sqrt(w4 * w4 + d1 * d1)
+    d1 = math.sqrt(w3 * w3 + dd * dd)
+    along_k = lmin == lmax
+    lo, hi = (kmin, kmax) if along_k else (lmin, lmax)
+    end2 = k2 if along_k else l2
+
+    def at(i):          # (l, k) 0-based index of position i along the side
+        return (l1 - 1, i - 1) if along_k else (i - 1, k1 - 1)
+
+    nd = float(hi - lo)
+    dtheta = theta1 - theta2
+    for ii in range(lo, hi + 1):
+        ij = hi + lo - ii if lo == end2 else ii
+        theta = theta1 - float(ii - lo) * dtheta / nd
+        dl = (d1 - d2) / dtheta
+        dl = d1 + dl * (theta - theta1)
+        rr[at(ij)] = r0 + dl * math.cos(theta)
+        ss[at(ij)] = s0 + dl * math.sin(theta)
+        bc[at(ij)] = seg["bc"]
+    rr[l1 - 1, k1 - 1] = r1
+    rr[l2 - 1, k2 - 1] = r2
+    ss[l1 - 1, k1 - 1] = s1
+    ss[l2 - 1, k2 - 1] = s2
+    if weighted:
+        for ii in range(lo, hi + 1):
+            ij = hi + lo - ii if lo == end2 else ii
+            rr[at(ij)] = theta1 - float(ii - lo) * dtheta / nd
+        while True:
+            done = True
+            for ii in range(lo + 1, hi):
+                d1 = w1 * rr[at(ii - 1)] + w2 * rr[at(ii + 1)] - rr[at(ii)]
+                if abs(d1) > tol:
+                    done = False
+                rr[at(ii)] = rr[at(ii)] + d1
+            if done:
+                break
+        for ii in range(lo + 1, hi):
+            theta = rr[at(ii)]
+            dl = (d1 - d2) / dtheta
+            dl = d1 + dl * (theta - theta1)
+            rr[at(ii)] = r0 + dl * math.cos(theta)
+            ss[at(ii)] = r0 + dl * math.sin(theta)
+    if fl:
+        for jj in range(0, (hi - lo) // 2 + 1):
+            a, b = at(lo + jj), at(hi - jj)
+            rr[a], rr[b] = rr[b], rr[a]
+            ss[a], ss[b] = ss[b], ss[a]
+
+
 def _stencil(x, w):
     """Residual of the relaxation stencil (setup_mesh.F90:851-860) at every
     interior point, evaluated left to right like the reference."""
@@ -170,13 +275,17 @@ def generate(mesh_nl, zerocut):
         st = str(segtyp[iseg - 1]).strip().upper()
         if st not in SEG_TYPES:
             raise DeckError("ERROR: unrecognised segment type")
-        if SEG_TYPES[st] not in (1, 5):
-            raise DeckError("ERROR: segment type %s not supported" % st)
+        if SEG_TYPES[st] == 4:
+            raise DeckError("ERROR: side_type is POINT but DJN off")
         b = str(segbc[iseg - 1]).strip().upper()
         if b not in BC_CODES:
             raise DeckError("ERROR: unrecognised segment boundary condition")
-        seg = {"point": [float(v) for v in segpos[iseg - 1, :]], "bc": BC_CODES[b]}
-        _side_line(rr, ss, bc, seg, ind, no_l, no_k, zerocut, tol, om, typ)
+        seg = {"point": [float(v) for v in segpos[iseg - 1, :]], "bc": BC_CODES[b],
+               "typ": SEG_TYPES[st]}
+        if SEG_TYPES[st] in (2, 3):
+            _side_arc(rr, ss, bc, seg, ind, no_l, no_k, zerocut, tol, om)
+        else:
+            _side_line(rr, ss, bc, seg, ind, no_l, no_k, zerocut, tol, om, typ)
     # interior initial guess (setup_mesh.F90:713-752)
     l1, k1, l2, k2 = 2, 2, no_l - 1, no_k - 1
     tl0, tl1, tk0, tk1 = rw[6], rw[1], rw[3], rw[4]

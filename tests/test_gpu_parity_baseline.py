@@ -154,8 +154,6 @@ def test_baseline_configuration(name, mode):
 def _deck_cases():
     out = []
     for name in golden.deck_names():
-        if "ARC_" in golden.deck_text(name):
-            continue   # curved sides: not set up by this harness yet
         out.append((name, 2 if name.endswith("_large") else 8 if name.endswith("_medium") else 20))
     return out
 
