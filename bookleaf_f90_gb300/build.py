@@ -5,7 +5,8 @@ Seven translation units, compiled in parallel with nvcc:
                  -DBL_FAST_ALGEBRA=1          algebraic identities allowed)
   bl_kernels.cu  -DBL_NS=exact --fmad=false  (bit-reproducible path)
   bl_capi.cu                                  (the C-ABI, host code)
-  bl_noalloc.cu                               (allocation-free getdt)
+  bl_noalloc.cu  --fmad=false                 (allocation-free getdt: the exact
+                                              build's k_getdt)
   bl_selftest.cu                              (FP64 self-test and rates)
   bl_diag.cu     --fmad=false                 (short print, Sod check)
   bl_mlp.cu                                   (the closure network, tensor cores)
@@ -64,7 +65,7 @@ def build(force=False, verbose=False, extra=()):
         (common + ["--fmad=false", "-DBL_NS=exact", "-c", os.path.join(CSRC, "bl_kernels.cu"),
                    "-o", os.path.join(BUILD, "k_exact.o")]),
         (common + ["-c", os.path.join(CSRC, "bl_capi.cu"), "-o", os.path.join(BUILD, "capi.o")]),
-        (common + ["--fmad=true", "-c", os.path.join(CSRC, "bl_noalloc.cu"),
+        (common + ["--fmad=false", "-c", os.path.join(CSRC, "bl_noalloc.cu"),
                    "-o", os.path.join(BUILD, "noalloc.o")]),
         (common + ["-c", os.path.join(CSRC, "bl_selftest.cu"), "-o", os.path.join(BUILD, "selftest.o")]),
         (common + ["--fmad=false", "-c", os.path.join(CSRC, "bl_diag.cu"),

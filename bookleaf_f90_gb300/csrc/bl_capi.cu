@@ -26,14 +26,16 @@ using bl::d4;
 
 namespace {
 
-const bl::Launchers kFast = {bl::fast::getdt_blocks,          bl::fast::launch_getdt,
+const bl::Launchers kFast = {bl::fast::getdt_blocks,          bl::fast::getdt_grid,
+                             bl::fast::launch_getdt,
                              bl::fast::launch_lag_force,       bl::fast::launch_lag_accel,
                              bl::fast::launch_lag_state,       bl::fast::launch_ale,
                              bl::fast::launch_getdt_batch,     bl::fast::launch_lag_force_batch,
                              bl::fast::launch_lag_accel_batch, bl::fast::launch_lag_state_batch,
                              bl::fast::launch_ale_batch,       bl::fast::prepare_mix_closure,
                              bl::fast::launch_mix_closure,     bl::fast::launch_mix_closure_batch};
-const bl::Launchers kExact = {bl::exact::getdt_blocks,          bl::exact::launch_getdt,
+const bl::Launchers kExact = {bl::exact::getdt_blocks,          bl::exact::getdt_grid,
+                              bl::exact::launch_getdt,
                               bl::exact::launch_lag_force,       bl::exact::launch_lag_accel,
                               bl::exact::launch_lag_state,       bl::exact::launch_ale,
                               bl::exact::launch_getdt_batch,     bl::exact::launch_lag_force_batch,
@@ -484,7 +486,7 @@ int init_impl(bl_ctx** out, const bl_sizes* sizes, const bl_config* config, void
     F.cutm_el = dalloc<double>(x, nel, st);
   }
   {
-    const int nblk = x->L.getdt_blocks(nel);
+    const int nblk = x->L.getdt_grid(nel);
     F.red_v = dalloc<double>(x, 2L * nblk, st);
     F.red_i = dalloc<int>(x, 2L * nblk, st);
   }

@@ -14,6 +14,7 @@ namespace bl {
 #define BL_DECLARE_LAUNCHERS(NS)                                                   \
   namespace NS {                                                                   \
   int getdt_blocks(int nel);                                                       \
+  int getdt_grid(int nel);                                                         \
   void launch_getdt(const DevFields& F, const DevCfg& C, cudaStream_t s);          \
   void launch_lag_force(const DevFields& F, const DevCfg& C, cudaStream_t s);      \
   void launch_lag_accel(const DevFields& F, const DevCfg& C, cudaStream_t s);      \
@@ -33,7 +34,8 @@ BL_DECLARE_LAUNCHERS(fast)
 BL_DECLARE_LAUNCHERS(exact)
 
 struct Launchers {
-  int (*getdt_blocks)(int);
+  int (*getdt_blocks)(int);  // k_getdt blocks of one mesh in a batch
+  int (*getdt_grid)(int);    // k_getdt grid (and partials) of a single mesh
   void (*getdt)(const DevFields&, const DevCfg&, cudaStream_t);
   void (*lag_force)(const DevFields&, const DevCfg&, cudaStream_t);
   void (*lag_accel)(const DevFields&, const DevCfg&, cudaStream_t);

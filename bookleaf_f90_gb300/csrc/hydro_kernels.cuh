@@ -525,10 +525,65 @@ __device__ __forceinline__ void div_max(double& v, int& i, double ov, int oi) {
 
 // hydro_dr_getcs2 (elcs2 += elvisc; mixed cells: sum frmass*(cpcs2+cpvisc)),
 // then the element's hydro_kn_getdtcfl and getdtdiv candidates
-__device__ __forceinline__ void getdt_tail(const DevFields& F, const DevCfg& C, int iel,
-                                           const double* x, const double* y, const double* u,
-                                           const double* v, double visc, double& cflv, int& cfli,
-                                           double& divv, int& divi) {
+// How k_getdt reads an element's connectivity and region and stores its
+// corner forces: in the library's own layout (0-based rows of four, face
+// numbers packed in one int, 32-byte corner vectors).  The exact-form
+// kernel takes the layout as a parameter, so that bl_getdt_noalloc runs the
+// same kernel on arrays in the reference's layout.
+struct DevLayout {
+  static __device__ __forceinline__ int4 nodes(const DevFields& F, int e) {
+    return __ldg(F.ielnd + e);
+  }
+  static __device__ __forceinline__ int4 nbrs(const DevFields& F, int e) {
+    return __ldg(F.ielel + e);
+  }
+  static __device__ __forceinline__ int faces(const DevFields& F, int e) {
+    return __ldg(F.ielfc + e);
+  }
+  static __device__ __forceinline__ int reg(const DevFields& F, int e) {
+    return __ldg(F.ielreg + e);
+  }
+  static __device__ __forceinline__ void corners(d4* p, int e, const double* q) {
+    p[e] = make_d4(q[0], q[1], q[2], q[3]);
+  }
+};
+
+// The element's squared CFL length of hydro_kn_getdtcfl (min over its
+// sides of geometry_kn_dlm or _dln), or -1 for a zdtnotreg region (the
+// reference's HUGE candidate); it does not depend on the viscosity.
+template <class L = DevLayout>
+__device__ __forceinline__ double getdt_cfl_len(const DevFields& F, const DevCfg& C, int iel,
+                                                const double* x, const double* y) {
+  const int ireg = L::reg(F, iel);
+  if (__ldg(C.zdtnotreg + ireg)) return -1.0;
+#if BL_FAST_ALGEBRA
+  return __ldg(C.zmidlength + ireg)
+             ? min_dlm(x, y)
+             : min_dln_iso(x, y, C.zcut, F.a1[iel], F.a2[iel], F.a3[iel], F.b1[iel], F.b2[iel],
+                           F.b3[iel]);
+#else
+  return __ldg(C.zmidlength + ireg) ? min_dlm(x, y) : min_dln(x, y, C.zcut);
+#endif
+}
+
+// hydro_kn_getdtdiv's candidate of the element
+__device__ __forceinline__ void getdt_div(const DevFields& F, int iel, const double* u,
+                                          const double* v, double& divv, int& divi) {
+  const double A1 = F.a1[iel], A3 = F.a3[iel], B1 = F.b1[iel], B3 = F.b3[iel];
+  double w1 = u[0] * (-B3 + B1) + v[0] * (A3 - A1) + u[1] * (B3 + B1) + v[1] * (-A3 - A1) +
+              u[2] * (B3 - B1) + v[2] * (-A3 + A1) + u[3] * (-B3 - B1) + v[3] * (A3 + A1);
+  w1 = DIV(absF(w1), F.vol[iel]);
+  if (gt_nn(w1, divv)) {  // divv is TINY or a larger positive value
+    divv = w1;
+    divi = iel;
+  }
+}
+
+// hydro_dr_getcs2 (elcs2 += elvisc; mixed cells: sum frmass*(cpcs2+cpvisc))
+// and the element's CFL candidate from its squared length len
+// (getdt_cfl_len)
+__device__ __forceinline__ void getdt_cfl(const DevFields& F, int iel, double len, double visc,
+                                          double& cflv, int& cfli) {
   double cs2v = F.cs2[iel] + visc;
   const int imx = F.elmx ? F.elmx[iel] : -1;
   if (imx >= 0) {
@@ -538,33 +593,24 @@ __device__ __forceinline__ void getdt_tail(const DevFields& F, const DevCfg& C, 
     cs2v = w1;
   }
   F.cs2v[iel] = cs2v;
-  // hydro_kn_getdtcfl
-  const int ireg = __ldg(F.ielreg + iel);
-  double r11;
-  if (__ldg(C.zdtnotreg + ireg)) {
-    r11 = DBL_MAX;
+  const double r11 = len < 0.0 ? DBL_MAX : DIV(len, cs2v);
+  if (cfli == 0x7fffffff) {
+    cflv = r11;
+    cfli = iel;
   } else {
-#if BL_FAST_ALGEBRA
-    double w1 = __ldg(C.zmidlength + ireg)
-                    ? min_dlm(x, y)
-                    : min_dln_iso(x, y, C.zcut, F.a1[iel], F.a2[iel], F.a3[iel], F.b1[iel],
-                                  F.b2[iel], F.b3[iel]);
-#else
-    double w1 = __ldg(C.zmidlength + ireg) ? min_dlm(x, y) : min_dln(x, y, C.zcut);
-#endif
-    r11 = DIV(w1, cs2v);
+    cfl_min(cflv, cfli, r11, iel);
   }
-  cflv = r11;
-  cfli = iel;
-  // hydro_kn_getdtdiv
-  const double A1 = F.a1[iel], A3 = F.a3[iel], B1 = F.b1[iel], B3 = F.b3[iel];
-  double w1 = u[0] * (-B3 + B1) + v[0] * (A3 - A1) + u[1] * (B3 + B1) + v[1] * (-A3 - A1) +
-              u[2] * (B3 - B1) + v[2] * (-A3 + A1) + u[3] * (-B3 - B1) + v[3] * (A3 + A1);
-  w1 = DIV(absF(w1), F.vol[iel]);
-  if (gt_nn(w1, divv)) {  // divv is TINY or a larger positive value
-    divv = w1;
-    divi = iel;
-  }
+}
+
+// hydro_dr_getcs2, then the element's hydro_kn_getdtcfl and getdtdiv
+// candidates
+template <class L = DevLayout>
+__device__ __forceinline__ void getdt_tail(const DevFields& F, const DevCfg& C, int iel,
+                                           const double* x, const double* y, const double* u,
+                                           const double* v, double visc, double& cflv, int& cfli,
+                                           double& divv, int& divi) {
+  getdt_cfl(F, iel, getdt_cfl_len<L>(F, C, iel, x, y), visc, cflv, cfli);
+  getdt_div(F, iel, u, v, divv, divi);
 }
 
 // The block reduction of the candidates, the last block's reduction of the
@@ -1005,7 +1051,7 @@ template <int BS>
 constexpr int getdt_elements_per_block() { return BS - 2; }
 #else
 
-template <int BS, bool BATCH>
+template <int BS, bool BATCH, class L = DevLayout>
 __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg C) {
   // the mesh of this block: the context's, or in a batch the block's own
   // (its blocks [blk0, blk0 + nblk), elements [el0, el1))
@@ -1032,7 +1078,7 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
   double divv = DBL_MIN;         // TINY(1.0)
   int divi = -1;
   if (iel < el1) {
-    const int4 nd = __ldg(F.ielnd + iel);
+    const int4 nd = L::nodes(F, iel);
     const int n[4] = {nd.x, nd.y, nd.z, nd.w};
     double x[4], y[4], u[4], v[4];
 #pragma unroll
@@ -1055,9 +1101,9 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
       // keeps the live state to the element's corners and the four edge
       // forces.  The faces of side s (neighbours across faces s and s+2)
       // are (s+3)&3 and s+1, in the reference's order 3, 1, 0, 2.
-      const int4 ee = __ldg(F.ielel + iel);
+      const int4 ee = L::nbrs(F, iel);
       const int nb[4] = {ee.x, ee.y, ee.z, ee.w};
-      const int fcp = __ldg(F.ielfc + iel);
+      const int fcp = L::faces(F, iel);
       const double cs2i = F.cs2[iel];
       const double xc = quarter(x[0] + x[1] + x[2] + x[3]);
       const double yc = quarter(y[0] + y[1] + y[2] + y[3]);
@@ -1100,7 +1146,7 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
           const int ins2 = e2 == 0 ? ((f2 + 3) & 3) : ((f2 + 1) & 3);
           double r1 = val1, r2 = val2;
           if (in1 != iel) {
-            const int4 m = __ldg(F.ielnd + in1);
+            const int4 m = L::nodes(F, in1);
             const int mm[4] = {m.x, m.y, m.z, m.w};
             const int a = mm[ins1], b = mm[(ins1 + 1) & 3];
             double ddx = F.ndx[b] - F.ndx[a], ddy = F.ndy[b] - F.ndy[a];
@@ -1110,7 +1156,7 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
             r1 = q * w1;
           }
           if (in2 != iel) {
-            const int4 m = __ldg(F.ielnd + in2);
+            const int4 m = L::nodes(F, in2);
             const int mm[4] = {m.x, m.y, m.z, m.w};
             const int a = mm[ins2], b = mm[(ins2 + 1) & 3];
             double ddx = F.ndx[b] - F.ndx[a], ddy = F.ndy[b] - F.ndy[a];
@@ -1165,13 +1211,13 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
       qy[1] = edy[1] - edy[0];
       qy[2] = edy[2] - edy[1];
       qy[3] = edy[3] - edy[2];
-      F.cnviscx[iel] = make_d4(qx[0], qx[1], qx[2], qx[3]);
-      F.cnviscy[iel] = make_d4(qy[0], qy[1], qy[2], qy[3]);
+      L::corners(F.cnviscx, iel, qx);
+      L::corners(F.cnviscy, iel, qy);
       F.visc[iel] = visc;
     } else {
       visc = F.visc[iel];
     }
-    getdt_tail(F, C, iel, x, y, u, v, visc, cflv, cfli, divv, divi);
+    getdt_tail<L>(F, C, iel, x, y, u, v, visc, cflv, cfli, divv, divi);
   }
   getdt_finish<BS, BATCH>(F, C, S, cflv, cfli, divv, divi, blk0, nblk, el0, I);
 }
@@ -1584,13 +1630,19 @@ static constexpr int BS_DT = 128;
 static constexpr int BS_EL = 128;
 static constexpr int BS_ND = 256;
 
+// one block per getdt_elements_per_block elements
 int getdt_blocks(int nel) {
   constexpr int E = getdt_elements_per_block<BS_DT>();
   return (nel + E - 1) / E;
 }
 
+// a single mesh's grid and number of partials: the same blocks (an equal
+// share per block over whole resident waves was measured slower: the SMs'
+// spread of finishing times is a spread of their speeds, not of their work)
+int getdt_grid(int nel) { return getdt_blocks(nel); }
+
 void launch_getdt(const DevFields& F, const DevCfg& C, cudaStream_t s) {
-  k_getdt<BS_DT, false><<<getdt_blocks(F.nel), BS_DT, 0, s>>>(F, C);
+  k_getdt<BS_DT, false><<<getdt_grid(F.nel), BS_DT, 0, s>>>(F, C);
 }
 void launch_lag_force(const DevFields& F, const DevCfg& C, cudaStream_t s) {
   k_lag_force<BS_EL, false><<<(F.nel + BS_EL - 1) / BS_EL, BS_EL, 0, s>>>(F, C);

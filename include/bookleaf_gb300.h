@@ -381,9 +381,10 @@ typedef struct {
  * for callers that cannot call cudaMalloc -- for example a host that hands
  * out every byte of device memory from its own pool, so that a library
  * allocating behind its back would fail or break its accounting.  It runs
- * the same computation as bl_getdt (edge viscosity, elcs2+elvisc, CFL and
- * divergence limits, time_dr_calc/time_dr_end) on arrays the caller passes,
- * without a bl_ctx.  Its reduction scratch is a fixed file-scope device
+ * bl_getdt's computation (edge viscosity, elcs2+elvisc, CFL and divergence
+ * limits, time_dr_calc/time_dr_end) on arrays the caller passes, without a
+ * bl_ctx: the library's own exact-form getdt kernel, so its results equal
+ * bl_getdt's in BL_FP_EXACT mode bit for bit.  Its reduction scratch is a fixed file-scope device
  * array, held by every GPU that loads the library until the process exits;
  * nothing is allocated or freed by this call.  The first call on a device
  * looks up that array's device address (cudaGetSymbolAddress); make that

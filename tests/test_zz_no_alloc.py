@@ -1,8 +1,12 @@
 """bl_getdt_noalloc: the allocation-free getdt for callers that cannot call
-cudaMalloc (a host that owns all device memory in its own pool, or work that
-must not allocate).  It is checked, through the C-ABI, against the existing
-entry point bl_getdt on the same state, on two calls in a row (the second
-call reuses the fixed scratch array the first one left behind).
+cudaMalloc (a host that owns all device memory in its own pool and hands it
+out itself).  It runs the library's exact-form k_getdt on arrays in the
+reference's layout, so it is checked, through the C-ABI, bit for bit
+against the existing entry point bl_getdt in exact mode and against the
+CPU restatement on the same state, on two calls in a row (the second call
+reuses the fixed scratch array the first one left behind): a single-region
+Sedov mesh, a 64x64 two-region mesh with zdtnotreg and zmidlength set, and
+a deck with the tensor viscosity switch (ztq, viscosity taken as given).
 
 This file is named so that pytest collects it last.
 """
@@ -27,7 +31,7 @@ class GetdtArrays(ct.Structure):
 
 def _state_after(deck, steps):
     p = Problem.from_deck(deck)
-    s = Solver(p, fp_mode=abi.FP_FAST)
+    s = Solver(p, fp_mode=abi.FP_EXACT)
     for _ in range(steps):
         assert s.step() == 0, s.error.message
     s.sync_to_host(0)
@@ -35,23 +39,42 @@ def _state_after(deck, steps):
     return p
 
 
-def test_noalloc_matches_getdt_twice():
+TWO_REGION = configs.sod(64, 64).replace(
+    "cvisc2=0.75\n", "cvisc2=0.75\n zmidlength(2)=.TRUE.\n zdtnotreg(1)=.TRUE.\n")
+TENSOR = configs.sod(64, 16).replace("cvisc2=0.75\n", "cvisc2=0.75\n visc='TENSOR'\n")
+CASES = {"sedov_24": (configs.sedov(24), 4), "sod_64x64_two_regions": (TWO_REGION, 6),
+         "sod_64x16_tensor": (TENSOR, 3)}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_noalloc_matches_getdt_and_oracle_twice(name):
     import torch
     from bookleaf_f90_gb300 import _lib
+    from oracle.oracle import Oracle
     L = _lib.load()
     L.bl_getdt_noalloc.argtypes = [ct.POINTER(GetdtArrays), ct.POINTER(abi.Config),
                                    ct.POINTER(abi.Timestep), ct.c_void_p, ct.POINTER(abi.Error)]
     L.bl_getdt_noalloc.restype = ct.c_int
     torch.cuda.init()
 
-    p = _state_after(configs.sedov(24), 4)
-    # the existing entry point on the same state
+    deck, steps = CASES[name]
+    p = _state_after(deck, steps)
+    if name == "sod_64x64_two_regions":
+        assert p.sizes.nreg == 2 and p.config.zdtnotreg[0] and p.config.zmidlength[1]
+    if name == "sod_64x16_tensor":
+        assert p.config.ztq
+    # the existing entry point (exact mode) and the CPU restatement on the
+    # same state
     q = p.copy()
-    sref = Solver(q, fp_mode=abi.FP_FAST)
+    sref = Solver(q, fp_mode=abi.FP_EXACT)
     ts_ref = q.timestep.copy()
     assert sref.inf_solver_getdt(ts_ref) == 0, sref.error.message
     sref.sync_to_host(0)
     sref.close()
+    o_p = p.copy()
+    ts_orc = o_p.timestep.copy()
+    orc = Oracle(o_p)
+    assert orc.getdt(ts_orc) == 0
 
     dev = torch.device("cuda:0")
     keep = []
@@ -63,16 +86,18 @@ def test_noalloc_matches_getdt_twice():
 
     f = p.fields
     outs = {k: torch.zeros(f[k].shape, dtype=torch.float64, device=dev)
-            for k in (abi.CNVISCX, abi.CNVISCY, abi.ELVISC)}
+            for k in (abi.CNVISCX, abi.CNVISCY)}
+    # the tensor switch takes elvisc as given: pass it in
+    outs[abi.ELVISC] = torch.from_numpy(f[abi.ELVISC].copy()).to(dev)
     cs2_out = torch.zeros(f[abi.ELCS2].shape, dtype=torch.float64, device=dev)
     A = GetdtArrays()
     A.nel, A.nnd = p.nel, p.nnd
-    for name, fid in (("ndx", abi.NDX), ("ndy", abi.NDY), ("ndu", abi.NDU), ("ndv", abi.NDV),
-                      ("indtype", abi.INDTYPE), ("ielnd", abi.IELND), ("ielel", abi.IELEL),
-                      ("ielfc", abi.IELFC), ("ielreg", abi.IELREG), ("eldensity", abi.ELDENSITY),
-                      ("elcs2", abi.ELCS2), ("a1", abi.A1), ("a3", abi.A3), ("b1", abi.B1),
-                      ("b3", abi.B3), ("elvolume", abi.ELVOLUME)):
-        setattr(A, name, d(f[fid]))
+    for nm, fid in (("ndx", abi.NDX), ("ndy", abi.NDY), ("ndu", abi.NDU), ("ndv", abi.NDV),
+                    ("indtype", abi.INDTYPE), ("ielnd", abi.IELND), ("ielel", abi.IELEL),
+                    ("ielfc", abi.IELFC), ("ielreg", abi.IELREG), ("eldensity", abi.ELDENSITY),
+                    ("elcs2", abi.ELCS2), ("a1", abi.A1), ("a3", abi.A3), ("b1", abi.B1),
+                    ("b3", abi.B3), ("elvolume", abi.ELVOLUME)):
+        setattr(A, nm, d(f[fid]))
     A.cnviscx = outs[abi.CNVISCX].data_ptr()
     A.cnviscy = outs[abi.CNVISCY].data_ptr()
     A.elvisc = outs[abi.ELVISC].data_ptr()
@@ -85,18 +110,44 @@ def test_noalloc_matches_getdt_twice():
         ierr = L.bl_getdt_noalloc(ct.byref(A), ct.byref(p.config), ct.byref(ts), None,
                                   ct.byref(err))
         assert ierr == 0, err.message
-        assert (ts.nstep, ts.idtel, ts.sdt) == (ts_ref.nstep, ts_ref.idtel, ts_ref.sdt), call
-        assert ts.dt == pytest.approx(ts_ref.dt, rel=1e-11)
-        assert ts.time == pytest.approx(ts_ref.time, rel=1e-11)
+        for ref in (ts_ref, ts_orc):
+            assert (ts.nstep, ts.idtel, ts.sdt, ts.dt, ts.time) == (
+                ref.nstep, ref.idtel, ref.sdt, ref.dt, ref.time), (call, ts.as_tuple())
         for fid, t in outs.items():
-            np.testing.assert_allclose(t.cpu().numpy(), q.fields[fid], rtol=1e-11, atol=1e-14)
-        np.testing.assert_allclose(cs2_out.cpu().numpy(), q.fields[abi.ELCS2], rtol=1e-11,
-                                   atol=1e-14)
+            got = t.cpu().numpy()
+            assert np.array_equal(got, q.fields[fid]), (call, abi.NAMES[fid])
+            assert np.array_equal(got, o_p.fields[fid]), (call, abi.NAMES[fid])
+        got = cs2_out.cpu().numpy()
+        # elcs2 + elvisc: bl_getdt and the restatement hold it in elcs2
+        assert np.array_equal(got, q.fields[abi.ELCS2]), call
+        assert np.array_equal(got, o_p.fields[abi.ELCS2]), call
         # clear the outputs so the second call has to write them again
-        for t in outs.values():
-            t.zero_()
+        # (elvisc is an input under the tensor switch)
+        outs[abi.CNVISCX].zero_()
+        outs[abi.CNVISCY].zero_()
+        if not p.config.ztq:
+            outs[abi.ELVISC].zero_()
         cs2_out.zero_()
         torch.cuda.synchronize()
+
+
+def test_noalloc_rejects_aliased_cs2():
+    from bookleaf_f90_gb300 import _lib
+    L = _lib.load()
+    L.bl_getdt_noalloc.argtypes = [ct.POINTER(GetdtArrays), ct.POINTER(abi.Config),
+                                   ct.POINTER(abi.Timestep), ct.c_void_p, ct.POINTER(abi.Error)]
+    L.bl_getdt_noalloc.restype = ct.c_int
+    A = GetdtArrays()
+    A.nel, A.nnd = 16, 25
+    for nm, _ in GetdtArrays._fields_[2:]:
+        setattr(A, nm, 4096)            # never dereferenced: rejected first
+    A.elcs2_out = A.elcs2
+    err = abi.Error()
+    ts = abi.Timestep()
+    cfg = abi.Config()
+    assert L.bl_getdt_noalloc(ct.byref(A), ct.byref(cfg), ct.byref(ts), None,
+                              ct.byref(err)) == abi.FAILURE
+    assert "alias" in err.message
 
 
 def test_noalloc_rejects_oversized_mesh():
