@@ -28,6 +28,7 @@
 #include <cmath>
 
 #include "bl_device.cuh"
+#include "bl_elem.cuh"
 #include "bl_fp64.cuh"
 #include "bl_kernels.h"
 #include "bl_mma.cuh"
@@ -119,27 +120,27 @@ __device__ __forceinline__ void eos_pc(const DevCfg& C, int mat, double rho, dou
     cs2 = C.ccut;
   } else if (t == 2) {
     double t1 = DIV(rho, __ldg(P + 2));
-    p = __ldg(P) * (pow(t1, __ldg(P + 1)) - 1.0);
+    p = __ldg(P) * (bl_pow(t1, __ldg(P + 1)) - 1.0);
     p = maxF(p, __ldg(P + 3));
     double t2 = __ldg(P + 1) - 1.0;
     cs2 = DIV(__ldg(P) * __ldg(P + 1), __ldg(P + 2));
-    cs2 = cs2 * pow(t1, t2);
+    cs2 = cs2 * bl_pow(t1, t2);
   } else if (t == 3) {
     double t1 = DIV(__ldg(P + 3) * __ldg(P + 5), rho);
     double t2 = DIV(__ldg(P + 4) * __ldg(P + 5), rho);
     double t3 = __ldg(P) * rho * e;
-    double t4 = (1.0 - DIV(__ldg(P), t1)) * __ldg(P + 1) * exp(-t1);
-    double t5 = (1.0 - DIV(__ldg(P), t2)) * __ldg(P + 2) * exp(-t2);
+    double t4 = (1.0 - DIV(__ldg(P), t1)) * __ldg(P + 1) * bl_exp(-t1);
+    double t5 = (1.0 - DIV(__ldg(P), t2)) * __ldg(P + 2) * bl_exp(-t2);
     p = t3 + t4 + t5;
     double pp = p;
     if (gt_nn(C.pcut, absF(pp))) pp = 0.0;
     double q1 = DIV(__ldg(P + 5), rho);
     double s3 = __ldg(P + 3) * q1;
     double u4 = DIV(__ldg(P), __ldg(P + 3)) + __ldg(P) * q1 - s3 * q1;
-    u4 = u4 * __ldg(P + 1) * exp(-s3);
+    u4 = u4 * __ldg(P + 1) * bl_exp(-s3);
     s3 = __ldg(P + 4) * q1;
     double u5 = DIV(__ldg(P), __ldg(P + 4)) + __ldg(P) * q1 - s3 * q1;
-    u5 = u5 * __ldg(P + 2) * exp(-s3);
+    u5 = u5 * __ldg(P + 2) * bl_exp(-s3);
     cs2 = DIV(__ldg(P) * pp, rho) + __ldg(P) * e - u4 - u5;
   } else {
     p = -1.0;

@@ -231,6 +231,72 @@ def sod_multimaterial(nx=100, ny=25, time_end=20.0, vf=0.5):
 """
 
 
+# The equations of state other than the ideal gas (eos_kn_forms.f90:28-106)
+# in a two-material tube: material 2 of the given form fills one half, with
+# a column of mixed cells (volume fraction vf) at the interface, material 1
+# is an ideal gas.  Parameters (eos_param(1:6,2)): void -- the pressure;
+# Tait -- B, gamma, rho0, the pressure floor (a water-like liquid, set
+# slightly below rho0 so that the floor holds ahead of the shock);
+# JWL -- omega, A, B, R1, R2, rho0 (TNT-like detonation products).
+EOS_FORMS = {
+    "void": ("VOID", (0.0,), "right", 0.01, 0.0),
+    "tait": ("TAIT", (3.0, 7.15, 1.0, -0.1), "right", 0.99, 0.0),
+    "jwl": ("JWL", (0.28, 3.712, 0.0323, 4.15, 0.95, 1.63), "left", 1.63, 1.0),
+}
+
+
+def eos_tube(form, nx=100, ny=10, time_end=20.0, vf=0.5):
+    """Two-material tube on [0,100]x[0,10] whose material 2 uses the EoS
+    form "void", "tait" or "jwl" (EOS_FORMS) over half of it; material 1 is
+    air (gamma 1.4) at rho 1, e 2.5 (p 1) where material 2 sits on the
+    right and at rho 0.125, e 2 (p 0.1) where it sits on the left."""
+    name, params, side, rho2, e2 = EOS_FORMS[form]
+    pl = "\n".join(" eos_param(%d,2)=%r" % (k + 1, v) for k, v in enumerate(params))
+    rect = "50.5,-10.0,150.0,50.0" if side == "right" else "-50.0,-10.0,49.5,50.0"
+    rho1, e1 = (1.0, 2.5) if side == "right" else (0.125, 2.0)
+    return f"""&CONTROL
+ time_start=0.0
+ time_end={time_end!r}
+ dt_initial=1.0e-3
+ dt_max=1.0e-1
+ dt_min=1.0e-8
+ dt_g=1.02
+ cfl_sf=0.5
+ cvisc1=0.5
+ cvisc2=0.75
+/
+&EOS
+ eos_type(1)='ideal gas'
+ eos_param(1,1)=1.4
+ eos_type(2)='{name}'
+{pl}
+/
+""" + _mesh(nx, ny, 0.0, 0.0, 100.0, 10.0, ("SLIPY", "SLIPX", "SLIPY", "SLIPX")) + f"""&INDICATORS
+ region_type(1)='background'
+ region_name(1)='tube'
+ material_type(1)='background'
+ material_name(1)='air'
+ material_type(2)='shape'
+ material_name(2)='{form}'
+ material_value(2)=1
+/
+&INITIAL_CONDITIONS
+ thermodynamic_type(1)='region'
+ thermodynamic_value(1)=1
+ density(1)={rho1!r}
+ energy(1)={e1!r}
+ thermodynamic_type(2)='material'
+ thermodynamic_value(2)=2
+ density(2)={rho2!r}
+ energy(2)={e2!r}
+/
+&SHAPES
+ shape_type(1)='rectangle'
+ shape_param(1,:)={rect},{vf!r}
+/
+"""
+
+
 def ensemble(n=512, seed=20240607, side_min=32, side_max=512):
     """Decks of a seeded ensemble of independent Eulerian problems: half Sod
     (gamma ~ U(1.2, 1.8), pressure ratio ~ logU(2, 1e4), density ratio 8,

@@ -19,6 +19,7 @@
  */
 #include <float.h>
 #include <math.h>
+#include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -362,6 +363,167 @@ static void density_dr_getdensity(orc_ctx *ctx) {
   if (ctx->s.ncp > 0) utils_kn_divide(ctx->s.ncp, R(BL_CPMASS), R(BL_CPVOLUME), R(BL_CPDENSITY));
 }
 
+/* ========================= exp, log, pow ================================= */
+/* The equations of state's exp and ** as this project evaluates them: the
+   same IEEE operations in the same order as the device's bl_exp, bl_log
+   and bl_pow (bookleaf_f90_gb300/csrc/bl_elem.cuh), so that the exact
+   device build and this restatement agree bit for bit; the reference's
+   gfortran takes these from the C library, which they follow to within
+   1-2 units in the last place (tests/test_oracle.py).  exp: Cody-Waite
+   reduction by ln 2 (40-bit head) and the Taylor series to r^13; log:
+   m 2^e with m in [sqrt(1/2), sqrt(2)), 2 atanh((m-1)/(m+1)) to s^23;
+   pow: exp(b log a) with log a and b log a as double-doubles (Dekker's
+   product, Knuth's two-sum) carried into exp's reduced argument. */
+static double orc_pow2i(int k) { /* 2^k, -1022 <= k <= 1023 */
+  uint64_t b = (uint64_t)(k + 1023) << 52;
+  double d;
+  memcpy(&d, &b, 8);
+  return d;
+}
+
+static double orc_exp2p(double x, double xl) {
+  if (x != x) return x;
+  if (x > 709.782712893384) return HUGE_VAL;
+  if (x < -745.1332191019412) return 0.0;
+  const double kd = nearbyint(x * 1.4426950408889634);
+  const double r = ((x - kd * 0.6931471805592082) - kd * 7.371002565167799e-13) + xl;
+  double p = 1.6059043836821613e-10;
+  p = p * r + 2.08767569878681e-09;
+  p = p * r + 2.505210838544172e-08;
+  p = p * r + 2.755731922398589e-07;
+  p = p * r + 2.7557319223985893e-06;
+  p = p * r + 2.48015873015873e-05;
+  p = p * r + 0.0001984126984126984;
+  p = p * r + 0.001388888888888889;
+  p = p * r + 0.008333333333333333;
+  p = p * r + 0.041666666666666664;
+  p = p * r + 0.16666666666666666;
+  p = p * r + 0.5;
+  const double q = r + (r * r) * p;
+  double e = 1.0 + q;
+  int k = (int)kd;
+  if (k > 1023) {
+    e = e * orc_pow2i(1023);
+    k -= 1023;
+  } else if (k < -1022) {
+    e = e * orc_pow2i(-1022);
+    k += 1022;
+    if (k < -1022) return 0.0;
+  }
+  return e * orc_pow2i(k);
+}
+
+double orc_exp(double x) { return orc_exp2p(x, 0.0); }
+
+static void orc_two_prod(double a, double b, double *p, double *e) {
+  *p = a * b;
+  double c = 134217729.0 * a;
+  const double ah = c - (c - a), al = a - ah;
+  c = 134217729.0 * b;
+  const double bh = c - (c - b), bl = b - bh;
+  *e = ((ah * bh - *p) + ah * bl + al * bh) + al * bl;
+}
+
+static void orc_log_dd(double a, double *hi, double *lo) {
+  uint64_t b;
+  memcpy(&b, &a, 8);
+  int e = 0;
+  if ((b >> 52) == 0) {
+    a = a * 18014398509481984.0;
+    memcpy(&b, &a, 8);
+    e = -54;
+  }
+  e += (int)((b >> 52) & 0x7ff) - 1023;
+  uint64_t mb = (b & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL;
+  double m;
+  memcpy(&m, &mb, 8);
+  if (m > 1.4142135623730951) {
+    m = m * 0.5;
+    e += 1;
+  }
+  const double f = m - 1.0;
+  const double uh = 2.0 + f, ul = f - (uh - 2.0);
+  const double s = f / uh;
+  double P, Pe;
+  orc_two_prod(s, uh, &P, &Pe);
+  const double serr = (((f - P) - Pe) - s * ul) / uh;
+  const double s2 = s * s;
+  double R = 0.043478260869565216;
+  R = R * s2 + 0.047619047619047616;
+  R = R * s2 + 0.05263157894736842;
+  R = R * s2 + 0.058823529411764705;
+  R = R * s2 + 0.06666666666666667;
+  R = R * s2 + 0.07692307692307693;
+  R = R * s2 + 0.09090909090909091;
+  R = R * s2 + 0.1111111111111111;
+  R = R * s2 + 0.14285714285714285;
+  R = R * s2 + 0.2;
+  R = R * s2 + 0.3333333333333333;
+  R = R * s2;
+  const double t = s + s;
+  const double ed = (double)e;
+  const double A = ed * 0.6931471805592082;
+  const double H = A + t;
+  const double bv = H - A;
+  const double L1 = (A - (H - bv)) + (t - bv);
+  *hi = H;
+  *lo = L1 + ((t * R + (serr + serr)) + ed * 7.371002565167799e-13);
+}
+
+double orc_log(double a) {
+  if (a != a) return a;
+  if (a <= 0.0) return a == 0.0 ? -HUGE_VAL : NAN;
+  if (a == HUGE_VAL) return a;
+  uint64_t b;
+  memcpy(&b, &a, 8);
+  int e = 0;
+  if ((b >> 52) == 0) {
+    a = a * 18014398509481984.0;
+    memcpy(&b, &a, 8);
+    e = -54;
+  }
+  e += (int)((b >> 52) & 0x7ff) - 1023;
+  uint64_t mb = (b & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL;
+  double m;
+  memcpy(&m, &mb, 8);
+  if (m > 1.4142135623730951) {
+    m = m * 0.5;
+    e += 1;
+  }
+  const double f = m - 1.0;
+  const double s = f / (2.0 + f);
+  const double s2 = s * s;
+  double R = 0.043478260869565216;
+  R = R * s2 + 0.047619047619047616;
+  R = R * s2 + 0.05263157894736842;
+  R = R * s2 + 0.058823529411764705;
+  R = R * s2 + 0.06666666666666667;
+  R = R * s2 + 0.07692307692307693;
+  R = R * s2 + 0.09090909090909091;
+  R = R * s2 + 0.1111111111111111;
+  R = R * s2 + 0.14285714285714285;
+  R = R * s2 + 0.2;
+  R = R * s2 + 0.3333333333333333;
+  R = R * s2;
+  const double t = s + s;
+  const double ed = (double)e;
+  return ed * 0.6931471805592082 + (t + (t * R + ed * 7.371002565167799e-13));
+}
+
+double orc_pow(double a, double b) {
+  if (b == 0.0 || a == 1.0) return 1.0;
+  if (a != a || b != b) return a + b;
+  if (a < 0.0) return NAN;
+  if (a == 0.0) return b > 0.0 ? 0.0 : HUGE_VAL;
+  if (a == HUGE_VAL) return b > 0.0 ? HUGE_VAL : 0.0;
+  double lh, ll;
+  orc_log_dd(a, &lh, &ll);
+  if (fabs(b) > 1e300 || fabs(lh * b) > 1e300) return orc_exp(b * lh);
+  double yh, yl;
+  orc_two_prod(b, lh, &yh, &yl);
+  return orc_exp2p(yh, yl + b * ll);
+}
+
 /* ========================= EoS =========================================== */
 
 #define EP(k, m) (cfg->eos_param[(m)][(k)-1])
@@ -375,15 +537,15 @@ static double eos_kn_getpressure(const bl_config *cfg, int mat, double density, 
     case 1: p = energy * density * (EP(1, imat) - 1.0); break;
     case 2:
       t1 = density / EP(3, imat);
-      p = EP(1, imat) * (pow(t1, EP(2, imat)) - 1.0);
+      p = EP(1, imat) * (orc_pow(t1, EP(2, imat)) - 1.0);
       p = maxF(p, EP(4, imat));
       break;
     case 3:
       t1 = EP(4, imat) * EP(6, imat) / density;
       t2 = EP(5, imat) * EP(6, imat) / density;
       t3 = EP(1, imat) * density * energy;
-      t4 = (1.0 - EP(1, imat) / t1) * EP(2, imat) * exp(-t1);
-      t5 = (1.0 - EP(1, imat) / t2) * EP(3, imat) * exp(-t2);
+      t4 = (1.0 - EP(1, imat) / t1) * EP(2, imat) * orc_exp(-t1);
+      t5 = (1.0 - EP(1, imat) / t2) * EP(3, imat) * orc_exp(-t2);
       p = t3 + t4 + t5;
       break;
     default: p = -1.0; break;
@@ -403,17 +565,17 @@ static double eos_kn_getcs2(const bl_config *cfg, int mat, double density, doubl
       t1 = density / EP(3, imat);
       t2 = EP(2, imat) - 1.0;
       cs2 = (EP(1, imat) * EP(2, imat)) / EP(3, imat);
-      cs2 = cs2 * pow(t1, t2);
+      cs2 = cs2 * orc_pow(t1, t2);
       break;
     case 3:
       t1 = EP(6, imat) / density;
       t2 = eos_kn_getpressure(cfg, imat, density, energy);
       t3 = EP(4, imat) * t1;
       t4 = EP(1, imat) / EP(4, imat) + EP(1, imat) * t1 - t3 * t1;
-      t4 = t4 * EP(2, imat) * exp(-t3);
+      t4 = t4 * EP(2, imat) * orc_exp(-t3);
       t3 = EP(5, imat) * t1;
       t5 = EP(1, imat) / EP(5, imat) + EP(1, imat) * t1 - t3 * t1;
-      t5 = t5 * EP(3, imat) * exp(-t3);
+      t5 = t5 * EP(3, imat) * orc_exp(-t3);
       cs2 = EP(1, imat) * t2 / density + EP(1, imat) * energy - t4 - t5;
       break;
     default: cs2 = cfg->ccut; break;

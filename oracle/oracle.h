@@ -54,6 +54,12 @@ void orc_sod_l1(int nel, double time, const double *volume,
 /* geometry_kn_getcentroid (geometry_kn_centroid.f90:29-55) */
 void orc_centroid(int nvert, const double *xx, const double *yy, double c[2]);
 
+/* exp, log and ** of the equations of state (eos_kn_forms.f90), evaluated
+ * with the same operations as the device's (see oracle.c) */
+double orc_exp(double x);
+double orc_log(double a);
+double orc_pow(double a, double b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -30,6 +30,11 @@ CASES = {
     "hourglass_subzonal": (HG, 20),
     "dtnotreg_midlength": (DTNOT, 15),
     "tensor_viscosity_off": (TENSOR, 10),
+    # the void, Tait and JWL equations of state (eos_kn_forms.f90:28-106),
+    # each for material 2 with a column of mixed cells
+    "eos_void": (configs.eos_tube("void", 60, 6), 20),
+    "eos_tait": (configs.eos_tube("tait", 60, 6), 20),
+    "eos_jwl": (configs.eos_tube("jwl", 60, 6), 20),
 }
 
 
@@ -41,7 +46,7 @@ def test_exact_per_phase(name):
 
 
 @pytest.mark.parametrize("name", ["sod_lag", "sedov_lag", "noh_eul", "sod_multimaterial",
-                                  "hourglass_subzonal"])
+                                  "hourglass_subzonal", "eos_tait", "eos_jwl"])
 def test_fast_within_tolerance(name):
     deck, n = CASES[name]
     pg, pc, bad = run_pair(deck, n, exact=False, phases=False, rtol=1e-9, atol=1e-12)

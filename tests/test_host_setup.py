@@ -32,6 +32,9 @@ DECKS = {
     "sod_multimaterial": configs.sod_multimaterial(40, 10),
     "hourglass_subzonal": HG,
     "dtnotreg_midlength": DTNOT,
+    "eos_void": configs.eos_tube("void", 30, 4),
+    "eos_tait": configs.eos_tube("tait", 30, 4),
+    "eos_jwl": configs.eos_tube("jwl", 30, 4),
 }
 
 
