@@ -259,7 +259,7 @@ def run_ensemble(args, torch):
     seed = 20240607
     K = args.steps if args.steps > 0 else 100
     W = max(1, args.warmup)
-    fp = abi.FP_EXACT if args.fp == "exact" else abi.FP_FAST
+    fp = {"exact": abi.FP_EXACT, "fast": abi.FP_FAST, "mixed": abi.FP_MIXED}[args.fp]
     items = configs.ensemble(n, seed=seed)
     t0 = time.perf_counter()
     probs = [Problem.from_deck(d) for d, _ in items]
@@ -399,7 +399,7 @@ def run_closure(args, torch):
     W warm-up steps and a re-upload of the initial state."""
     import functools
     from bookleaf_f90_gb300 import Problem, Solver, abi, closure, configs
-    fp = abi.FP_EXACT if args.fp == "exact" else abi.FP_FAST
+    fp = {"exact": abi.FP_EXACT, "fast": abi.FP_FAST, "mixed": abi.FP_MIXED}[args.fp]
     nx = args.size or 800
     ny = max(1, nx // 10)
     W = max(1, args.warmup)
@@ -574,7 +574,7 @@ def run_closure_ensemble(args, torch):
     import ctypes as ct
     import functools
     from bookleaf_f90_gb300 import BatchSolver, Problem, Solver, abi, closure, configs
-    fp = abi.FP_EXACT if args.fp == "exact" else abi.FP_FAST
+    fp = {"exact": abi.FP_EXACT, "fast": abi.FP_FAST, "mixed": abi.FP_MIXED}[args.fp]
     n = args.size or 64
     seed = 20240613
     W = max(1, args.warmup)
@@ -724,7 +724,7 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--workload", default="sedov")
     ap.add_argument("--size", type=int, default=0)
-    ap.add_argument("--fp", default="fast", choices=["fast", "exact"])
+    ap.add_argument("--fp", default="fast", choices=["fast", "exact", "mixed"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
@@ -802,7 +802,7 @@ def main():
 
     base = Problem.from_deck(deck)
     nel = base.nel
-    fp = abi.FP_EXACT if args.fp == "exact" else abi.FP_FAST
+    fp = {"exact": abi.FP_EXACT, "fast": abi.FP_FAST, "mixed": abi.FP_MIXED}[args.fp]
 
     # ---------------- value: device-resident time loop ---------------------
     # W warm-up steps (graph capture, caches), then the initial state is

@@ -31,7 +31,7 @@ globals().update(IDS)
 NAMES = {v: k.lower() for k, v in IDS.items()}
 
 SUCCESS, FAILURE, HALT_ALL, HALT_SINGLE = 0, -1, 1, 2
-FP_FAST, FP_EXACT = 0, 1
+FP_FAST, FP_EXACT, FP_MIXED = 0, 1, 2
 DT_NAMES = [" MAXIMUM", "  GROWTH", " INITIAL", "     CFL", "     DIV"]
 
 

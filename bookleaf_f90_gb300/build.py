@@ -1,9 +1,11 @@
 """Build the sm_103a shared library libbookleaf_gb300.so in-tree.
 
-Seven translation units, compiled in parallel with nvcc:
+Eight translation units, compiled in parallel with nvcc:
   bl_kernels.cu  -DBL_NS=fast  --fmad=true   (fused multiply-add and exact
                  -DBL_FAST_ALGEBRA=1          algebraic identities allowed)
   bl_kernels.cu  -DBL_NS=exact --fmad=false  (bit-reproducible path)
+  bl_kernels.cu  -DBL_NS=mixed --fmad=true   (the fast build with the limiter
+                 -DBL_MIXED=1                 arithmetic in FP32)
   bl_capi.cu                                  (the C-ABI, host code)
   bl_noalloc.cu  --fmad=false                 (allocation-free getdt: the exact
                                               build's k_getdt)
@@ -64,6 +66,8 @@ def build(force=False, verbose=False, extra=()):
                    "-o", os.path.join(BUILD, "k_fast.o")]),
         (common + ["--fmad=false", "-DBL_NS=exact", "-c", os.path.join(CSRC, "bl_kernels.cu"),
                    "-o", os.path.join(BUILD, "k_exact.o")]),
+        (common + ["--fmad=true", "-DBL_NS=mixed", "-DBL_FAST_ALGEBRA=1", "-DBL_MIXED=1", "-c",
+                   os.path.join(CSRC, "bl_kernels.cu"), "-o", os.path.join(BUILD, "k_mixed.o")]),
         (common + ["-c", os.path.join(CSRC, "bl_capi.cu"), "-o", os.path.join(BUILD, "capi.o")]),
         (common + ["--fmad=false", "-c", os.path.join(CSRC, "bl_noalloc.cu"),
                    "-o", os.path.join(BUILD, "noalloc.o")]),
@@ -88,6 +92,7 @@ def build(force=False, verbose=False, extra=()):
     subprocess.check_call([cc] + ARCH + ["-shared", "-cudart", "static", "-o", tmp,
                                          os.path.join(BUILD, "k_fast.o"),
                                          os.path.join(BUILD, "k_exact.o"),
+                                         os.path.join(BUILD, "k_mixed.o"),
                                          os.path.join(BUILD, "capi.o"),
                                          os.path.join(BUILD, "noalloc.o"),
                                          os.path.join(BUILD, "selftest.o"),

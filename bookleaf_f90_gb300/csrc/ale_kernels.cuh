@@ -71,6 +71,34 @@ __device__ __forceinline__ bool prod_le0(double w1, double w2) {
 #endif
 }
 
+#if BL_MIXED
+// Mixed build: the remap limiters' gradient in FP32.  For the differences
+// A, B of the advected variable towards the two neighbours and the masses
+// (or volumes) mA, mB of the two sides, w8 = (A mB^2 + B mA^2) /
+// (mA mB (mA + mB)) and |grad| = min(|w8|, |A|/mA, |B|/mB), zero unless A
+// and B have the same sign, with the sign of S.  The operands are brought
+// into FP32's range by powers of two taken from their exponents (exact),
+// and the result scaled back in FP64.
+__device__ __forceinline__ int exp_of(double x) {
+  return (int)((bits64(x) >> 52) & 0x7ff) - 1023;
+}
+__device__ __forceinline__ double pow2c(int k) {  // 2^k, k clamped to the normal range
+  k = k < -1022 ? -1022 : (k > 1023 ? 1023 : k);
+  return from_bits64((long long)(k + 1023) << 52);
+}
+__device__ __forceinline__ double grad_f32(double A, double B, double mA, double mB, double S) {
+  if (prod_le0(A, B)) return 0.0;
+  const int ev = exp_of(maxF_nn(absF(A), absF(B)));
+  const int em = exp_of(maxF_nn(mA, mB));
+  const double sv = pow2c(-ev), sm = pow2c(-em);
+  const float a = (float)(A * sv), b = (float)(B * sv);
+  const float ma = (float)(mA * sm), mb = (float)(mB * sm);
+  const float w8 = (a * mb * mb + b * ma * ma) / (ma * mb * (ma + mb));
+  const float g = fminf(fminf(fabsf(w8), fabsf(a) / ma), fabsf(b) / mb);
+  return signF((double)g * pow2c(ev) * pow2c(-em), S);
+}
+#endif
+
 // The limited face flux of ale_kn_fluxelvl for the pair (i1, i2=i1+2),
 // returning (fcflux(i1), fcflux(i2)) (ale_kn_advectors.f90:48-78).
 __device__ __forceinline__ void elvl_pair(int iel, int i1, const int* nb, const int* fc,
@@ -88,10 +116,14 @@ __device__ __forceinline__ void elvl_pair(int iel, int i1, const int* nb, const 
   double w6 = r4 + cget(cnbasis, iel1, j2) + cget(cnbasis, iel1, (j2 + 1) & 3);
   double w1 = rv - elvar[iel2];
   double w2 = elvar[iel1] - rv;
+#if BL_MIXED
+  const double grad = grad_f32(w1, w2, w5, w6, w2);
+#else
   double w3 = absF(w1), w4 = absF(w2);
   double w8 = DIV(w1 * w6 * w6 + w2 * w5 * w5, w5 * w6 * (w5 + w6));
   double grad = sign_of(minF(minF(absF(w8), DIV(w3, w5)), DIV(w4, w6)), w2);
   if (prod_le0(w1, w2)) grad = 0.0;
+#endif
   o1 = r1 * (rv + grad * (r3 - half(r1)));
   o2 = r2 * (rv - grad * (r4 - half(r2)));
   (void)iel;
@@ -292,9 +324,14 @@ __global__ void __launch_bounds__(BS) k_ale_el(DevFields F, DevCfg C) {
           const double* nvar = q == 0 ? F.ndu : F.ndv;
           const double rv = cvar[nearc];
           const double I = cvar[farc] - rv, O = rv - nvar[nbn];
+#if BL_MIXED
+          const double grad = grad_f32(I, O, w5, w6, I);
+          (void)den;
+#else
           const double w8 = DIV(I * w6 * w6 + O * w5 * w5, den);
           double grad = sign_of(minF(minF(absF(w8), DIV(absF(O), w6)), DIV(absF(I), w5)), I);
           if (prod_le0(O, I)) grad = 0.0;
+#endif
           const double rd = cdb * (rv + grad * rd0);
           if (q == 0) rdu = rd; else rdv = rd;
         }

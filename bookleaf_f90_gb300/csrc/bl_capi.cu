@@ -42,6 +42,14 @@ const bl::Launchers kExact = {bl::exact::getdt_blocks,          bl::exact::getdt
                               bl::exact::launch_lag_accel_batch, bl::exact::launch_lag_state_batch,
                               bl::exact::launch_ale_batch,       bl::exact::prepare_mix_closure,
                               bl::exact::launch_mix_closure,     bl::exact::launch_mix_closure_batch};
+const bl::Launchers kMixed = {bl::mixed::getdt_blocks,          bl::mixed::getdt_grid,
+                              bl::mixed::launch_getdt,
+                              bl::mixed::launch_lag_force,       bl::mixed::launch_lag_accel,
+                              bl::mixed::launch_lag_state,       bl::mixed::launch_ale,
+                              bl::mixed::launch_getdt_batch,     bl::mixed::launch_lag_force_batch,
+                              bl::mixed::launch_lag_accel_batch, bl::mixed::launch_lag_state_batch,
+                              bl::mixed::launch_ale_batch,       bl::mixed::prepare_mix_closure,
+                              bl::mixed::launch_mix_closure,     bl::mixed::launch_mix_closure_batch};
 
 // batches (defined with bl_init_batch below)
 void batch_copy(bl_ctx* x, int id, bool to_mesh);
@@ -254,6 +262,10 @@ int init_impl(bl_ctx** out, const bl_sizes* sizes, const bl_config* config, void
     return BL_FAILURE;
   }
   *out = nullptr;
+  if (fp_mode != BL_FP_FAST && fp_mode != BL_FP_EXACT && fp_mode != BL_FP_MIXED) {
+    set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init: unknown fp_mode");
+    return BL_FAILURE;
+  }
   int ndev = 0;
   cudaError_t r = cudaGetDeviceCount(&ndev);
   if (r != cudaSuccess || ndev < 1) {
@@ -360,7 +372,7 @@ int init_impl(bl_ctx** out, const bl_sizes* sizes, const bl_config* config, void
   x->s = s;
   x->c = c;
   x->fp_mode = fp_mode;
-  x->L = (fp_mode == BL_FP_EXACT) ? kExact : kFast;
+  x->L = (fp_mode == BL_FP_EXACT) ? kExact : (fp_mode == BL_FP_MIXED) ? kMixed : kFast;
   for (int id = 1; id <= BL_NID; id++) x->host[id] = dh[id];
   x->ielmat_h.assign(ielmat, ielmat + nel);
   cudaGetDevice(&x->device);

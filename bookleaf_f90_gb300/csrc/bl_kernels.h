@@ -1,8 +1,9 @@
 // bl_kernels.h -- launch functions of the kernel translation unit.
 //
-// bl_kernels.cu is compiled twice: once as namespace bl::exact with
-// --fmad=false (bit-reproducible against a -ffp-contract=off CPU build) and
-// once as namespace bl::fast with --fmad=true.  The C-ABI layer picks one
+// bl_kernels.cu is compiled three times: as namespace bl::exact with
+// --fmad=false (bit-reproducible against a -ffp-contract=off CPU build), as
+// bl::fast with --fmad=true, and as bl::mixed, the fast build with the
+// limiter and edge-viscosity arithmetic in FP32 (BL_MIXED, bl_lreal.cuh).  The C-ABI layer picks one
 // table per context (bl_init's fp_mode).
 #pragma once
 #include <cuda_runtime.h>
@@ -32,6 +33,7 @@ namespace bl {
 
 BL_DECLARE_LAUNCHERS(fast)
 BL_DECLARE_LAUNCHERS(exact)
+BL_DECLARE_LAUNCHERS(mixed)
 
 struct Launchers {
   int (*getdt_blocks)(int);  // k_getdt blocks of one mesh in a batch

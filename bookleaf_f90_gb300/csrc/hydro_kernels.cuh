@@ -30,6 +30,7 @@
 #include "bl_device.cuh"
 #include "bl_elem.cuh"
 #include "bl_fp64.cuh"
+#include "bl_lreal.cuh"
 #include "bl_kernels.h"
 #include "bl_mma.cuh"
 
@@ -258,26 +259,27 @@ __device__ __forceinline__ double min_dln(const double* x, const double* y, doub
 // (a1,b1); so the reference's distpl/denom is 4 X^2 / Y with X = dx*q -
 // dy*p and Y = dx^2 + dy^2 (exact in real arithmetic), and its denominator
 // is 4 Y.  A degenerate opposite edge (4 Y < zcut) takes the corner form.
-__device__ __forceinline__ double min_dln_iso(const double* x, const double* y, double zcut,
-                                              double a1, double a2, double a3, double b1,
-                                              double b2, double b3) {
-  const double dxs[4] = {a1 + a2, a2 - a3, a1 - a2, a2 + a3};
-  const double dys[4] = {b1 + b2, b2 - b3, b1 - b2, b2 + b3};
-  double r[4];
+// (T: FP64, or FP32 in the mixed build)
+template <class T>
+__device__ __forceinline__ T min_dln_iso(const double* x, const double* y, T zcut, T a1, T a2,
+                                         T a3, T b1, T b2, T b3) {
+  const T dxs[4] = {a1 + a2, a2 - a3, a1 - a2, a2 + a3};
+  const T dys[4] = {b1 + b2, b2 - b3, b1 - b2, b2 + b3};
+  T r[4];
 #pragma unroll
   for (int k = 0; k < 4; k++) {
-    const double dx = dxs[k], dy = dys[k];
-    const double p = (k & 1) ? a1 : a3, q = (k & 1) ? b1 : b3;
-    const double Y = dx * dx + dy * dy;
+    const T dx = dxs[k], dy = dys[k];
+    const T p = (k & 1) ? a1 : a3, q = (k & 1) ? b1 : b3;
+    const T Y = dx * dx + dy * dy;
     if (gt_nn(zcut, times4(Y))) {
       const int a = k, b = (k + 1) & 3, c = (k + 2) & 3;
-      r[k] = g_distpp(x[a], y[a], x[b], y[b], x[c], y[c]);
+      r[k] = (T)g_distpp(x[a], y[a], x[b], y[b], x[c], y[c]);
     } else {
-      const double X = dx * q - dy * p;
+      const T X = dx * q - dy * p;
       r[k] = DIV(times4(X * X), Y);
     }
   }
-  double m = r[0];
+  T m = r[0];
   m = minF_nn(m, r[1]);
   m = minF_nn(m, r[2]);
   m = minF_nn(m, r[3]);
@@ -560,8 +562,9 @@ __device__ __forceinline__ double getdt_cfl_len(const DevFields& F, const DevCfg
 #if BL_FAST_ALGEBRA
   return __ldg(C.zmidlength + ireg)
              ? min_dlm(x, y)
-             : min_dln_iso(x, y, C.zcut, F.a1[iel], F.a2[iel], F.a3[iel], F.b1[iel], F.b2[iel],
-                           F.b3[iel]);
+             : (double)min_dln_iso<lr>(x, y, lr_cut(C.zcut), (lr)F.a1[iel], (lr)F.a2[iel],
+                                       (lr)F.a3[iel], (lr)F.b1[iel], (lr)F.b2[iel],
+                                       (lr)F.b3[iel]);
 #else
   return __ldg(C.zmidlength + ireg) ? min_dlm(x, y) : min_dln(x, y, C.zcut);
 #endif
@@ -570,10 +573,18 @@ __device__ __forceinline__ double getdt_cfl_len(const DevFields& F, const DevCfg
 // hydro_kn_getdtdiv's candidate of the element
 __device__ __forceinline__ void getdt_div(const DevFields& F, int iel, const double* u,
                                           const double* v, double& divv, int& divi) {
+#if BL_MIXED
+  const lr A1 = (lr)F.a1[iel], A3 = (lr)F.a3[iel], B1 = (lr)F.b1[iel], B3 = (lr)F.b3[iel];
+  lr wl = (lr)u[0] * (-B3 + B1) + (lr)v[0] * (A3 - A1) + (lr)u[1] * (B3 + B1) +
+          (lr)v[1] * (-A3 - A1) + (lr)u[2] * (B3 - B1) + (lr)v[2] * (-A3 + A1) +
+          (lr)u[3] * (-B3 - B1) + (lr)v[3] * (A3 + A1);
+  const double w1 = (double)DIV(absF(wl), (lr)F.vol[iel]);
+#else
   const double A1 = F.a1[iel], A3 = F.a3[iel], B1 = F.b1[iel], B3 = F.b3[iel];
   double w1 = u[0] * (-B3 + B1) + v[0] * (A3 - A1) + u[1] * (B3 + B1) + v[1] * (-A3 - A1) +
               u[2] * (B3 - B1) + v[2] * (-A3 + A1) + u[3] * (-B3 - B1) + v[3] * (A3 + A1);
   w1 = DIV(absF(w1), F.vol[iel]);
+#endif
   if (gt_nn(w1, divv)) {  // divv is TINY or a larger positive value
     divv = w1;
     divi = iel;
@@ -594,7 +605,11 @@ __device__ __forceinline__ void getdt_cfl(const DevFields& F, int iel, double le
     cs2v = w1;
   }
   F.cs2v[iel] = cs2v;
+#if BL_MIXED
+  const double r11 = len < 0.0 ? DBL_MAX : (double)DIV((lr)len, (lr)cs2v);
+#else
   const double r11 = len < 0.0 ? DBL_MAX : DIV(len, cs2v);
+#endif
   if (cfli == 0x7fffffff) {
     cflv = r11;
     cfli = iel;
@@ -777,32 +792,38 @@ __device__ __forceinline__ void getdt_finish(const DevFields& F, const DevCfg& C
 // differences; the face vectors' projections on their own unit vectors
 // are |d|^2 / max(|d|, zerocut) (exact in real arithmetic, never negative,
 // so the reference's sign guards drop out).
+// (in lr: FP64, or FP32 in the mixed build)
 struct FaceQ {
-  double du, dv, lu, lx, uh, vh, xh, yh, w1;
+  lr du, dv, lu, lx, uh, vh, xh, yh, w1;
 };
-__device__ __forceinline__ FaceQ face_q(double du, double dv, double dx, double dy, double zc) {
+__device__ __forceinline__ FaceQ face_q(lr du, lr dv, lr dx, lr dy, lr zc) {
   FaceQ f;
   f.du = du;
   f.dv = dv;
-  const double squ = du * du + dv * dv, sqx = dx * dx + dy * dy;
+  const lr squ = du * du + dv * dv, sqx = dx * dx + dy * dy;
   f.lu = SQRT(squ);
   f.lx = SQRT(sqx);
-  const double ru = DIV(1.0, maxF_nn(f.lu, zc)), rx = DIV(1.0, maxF_nn(f.lx, zc));
+  const lr ru = DIV((lr)1, maxF_nn(f.lu, zc)), rx = DIV((lr)1, maxF_nn(f.lx, zc));
   f.uh = du * ru;
   f.vh = dv * ru;
   f.xh = dx * rx;
   f.yh = dy * rx;
-  const double w1 = DIV(squ * ru, maxF_nn(sqx * rx, zc));
-  f.w1 = DIV(1.0, maxF_nn(w1, zc));
+  const lr w1 = DIV(squ * ru, maxF_nn(sqx * rx, zc));
+  f.w1 = DIV((lr)1, maxF_nn(w1, zc));
   return f;
 }
 // limiter ratio of a neighbour face with differences (ddx, ddy, ddu, ddv)
 // against face f (hydro_kn_edgeviscosity.f90:117-151)
-__device__ __forceinline__ double nb_ratio(const FaceQ& f, double ddx, double ddy, double ddu,
-                                           double ddv, double zc) {
-  const double dn = ddx * f.xh + ddy * f.yh;
-  const double q = DIV(ddu * f.uh + ddv * f.vh, signF(maxF_nn(absF(dn), zc), dn));
+__device__ __forceinline__ lr nb_ratio(const FaceQ& f, lr ddx, lr ddy, lr ddu, lr ddv, lr zc) {
+  const lr dn = ddx * f.xh + ddy * f.yh;
+  const lr q = DIV(ddu * f.uh + ddv * f.vh, signF(maxF_nn(absF(dn), zc), dn));
+#if BL_MIXED
+  // FP32 saturates where FP64 would not: keep the ratio finite (the
+  // limiter only distinguishes r below 0, in [0, 1] and above 1)
+  return fmaxf(fminf(q * f.w1, 1e30f), -1e30f);
+#else
   return q * f.w1;
+#endif
 }
 
 // k_getdt of the fast build shares face work between neighbouring threads.
@@ -854,9 +875,9 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
   // factors that do not depend on the side the face is seen from,
   // cvisc1*sqrt((cs2 + cs2')/2) + cvisc2*|du| and rho + rho' (the same sums
   // with the operands swapped, which IEEE addition does not change)
-  __shared__ double s_f0[11][BS];
-  __shared__ double s_fd[8][BS];  // faces 1, 3: dx dy du dv each
-  const double zc = C.zerocut;
+  __shared__ lr s_f0[11][BS];
+  __shared__ lr s_fd[8][BS];  // faces 1, 3: dx dy du dv each
+  const lr zl = lr_cut(C.zerocut);
   int n[4] = {0, 0, 0, 0};
   double x[4], y[4], u[4], v[4];
   if (inmesh) {
@@ -875,7 +896,8 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
   }
   if (!C.ztq) {
     if (inmesh) {
-      const FaceQ f0 = face_q(u[1] - u[0], v[1] - v[0], x[1] - x[0], y[1] - y[0], zc);
+      const FaceQ f0 = face_q((lr)(u[1] - u[0]), (lr)(v[1] - v[0]), (lr)(x[1] - x[0]),
+                              (lr)(y[1] - y[0]), zl);
       s_f0[0][t] = f0.du;
       s_f0[1][t] = f0.dv;
       s_f0[2][t] = f0.lu;
@@ -886,8 +908,8 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
       s_f0[7][t] = f0.yh;
       s_f0[8][t] = f0.w1;
       const int nb0 = __ldg(F.ielel + iel).x;
-      s_f0[9][t] = C.cvisc1 * SQRT(half(F.cs2[iel] + F.cs2[nb0])) + C.cvisc2 * f0.lu;
-      s_f0[10][t] = F.rho[iel] + F.rho[nb0];
+      s_f0[9][t] = (lr)C.cvisc1 * SQRT((lr)half(F.cs2[iel] + F.cs2[nb0])) + (lr)C.cvisc2 * f0.lu;
+      s_f0[10][t] = (lr)(F.rho[iel] + F.rho[nb0]);
       s_fd[0][t] = x[2] - x[1];
       s_fd[1][t] = y[2] - y[1];
       s_fd[2][t] = u[2] - u[1];
@@ -913,25 +935,25 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
       // the vector from an edge's midpoint to the centroid is (a3,b3),
       // (-a1,-b1), (-a3,-b3), (a1,b1) for faces 0..3 (corners written as
       // s -+ a1 +- a2 -+ a3, exact in real arithmetic)
-      const double ga1 = F.a1[iel], ga3 = F.a3[iel], gb1 = F.b1[iel], gb3 = F.b3[iel];
+      const lr ga1 = (lr)F.a1[iel], ga3 = (lr)F.a3[iel], gb1 = (lr)F.b1[iel], gb3 = (lr)F.b3[iel];
       // |c|^2 of faces 1,3 and of faces 0,2 (only the cut test uses it)
-      const double c1sq = ga1 * ga1 + gb1 * gb1, c3sq = ga3 * ga3 + gb3 * gb3;
+      const lr c1sq = ga1 * ga1 + gb1 * gb1, c3sq = ga3 * ga3 + gb3 * gb3;
       // max over faces of edv * |du|; the reference's max of
       // edv * 2|du| / max(rho, zerocut) is that times 2 / max(rho, zerocut)
-      double vmax = 0.0;
-      double edx[4], edy[4];
+      lr vmax = (lr)0;
+      lr edx[4], edy[4];
 #pragma unroll
       for (int s = 0; s < 2; s++) {
         const int in1 = nb[s], in2 = nb[s + 2];
         const int f1 = fc_of(fcp, s), f2 = fc_of(fcp, s + 2);
         // boundary rule (hydro_kn_edgeviscosity.f90:154-183)
-        double val1 = 0.0, val2 = 0.0;
+        lr val1 = (lr)0, val2 = (lr)0;
         if (in1 == iel)
           val1 = (__ldg(F.indtype + n[s]) < 0 && __ldg(F.indtype + n[(s + 1) & 3]) < 0 && in2 != iel)
-                     ? 1.0 : 0.0;
+                     ? (lr)1 : (lr)0;
         if (in2 == iel)
           val2 = (__ldg(F.indtype + n[s + 2]) < 0 && __ldg(F.indtype + n[(s + 3) & 3]) < 0 &&
-                  in1 != iel) ? 1.0 : 0.0;
+                  in1 != iel) ? (lr)1 : (lr)0;
 #pragma unroll
         for (int e2 = 0; e2 < 2; e2++) {
           const int is = e2 == 0 ? ((s + 3) & 3) : (s + 1);
@@ -963,23 +985,24 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
               f.yh = negF(s_f0[7][q]);
               f.w1 = s_f0[8][q];
             } else {
-              f = face_q(u[3] - u[2], v[3] - v[2], x[3] - x[2], y[3] - y[2], zc);
+              f = face_q((lr)(u[3] - u[2]), (lr)(v[3] - v[2]), (lr)(x[3] - x[2]),
+                         (lr)(y[3] - y[2]), zl);
             }
           } else {
             const int o = is == 1 ? 0 : 4;
-            f = face_q(s_fd[o + 2][t], s_fd[o + 3][t], s_fd[o][t], s_fd[o + 1][t], zc);
+            f = face_q(s_fd[o + 2][t], s_fd[o + 3][t], s_fd[o][t], s_fd[o + 1][t], zl);
           }
           // neighbour faces: edge 1 uses MOD(ielfc,4)+1 / MOD(ielfc+2,4)+1,
           // edge 2 the other pair (hydro_kn_edgeviscosity.f90:117-151)
           const int ins1 = e2 == 0 ? ((f1 + 1) & 3) : ((f1 + 3) & 3);
           const int ins2 = e2 == 0 ? ((f2 + 3) & 3) : ((f2 + 1) & 3);
-          double r1 = val1, r2 = val2;
+          lr r1 = val1, r2 = val2;
 #pragma unroll
           for (int k = 0; k < 2; k++) {
             const int inb = k == 0 ? in1 : in2;
             const int ins = k == 0 ? ins1 : ins2;
             if (inb == iel) continue;
-            double ddx, ddy, ddu, ddv;
+            lr ddx, ddy, ddu, ddv;
             const int o = inb - iel;
             if ((o == 1 || o == -1) && (ins & 1)) {
               const int q = t + o, c = ins == 1 ? 0 : 4;
@@ -996,47 +1019,46 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
               ddu = F.ndu[b] - F.ndu[a];
               ddv = F.ndv[b] - F.ndv[a];
             }
-            const double r = nb_ratio(f, ddx, ddy, ddu, ddv, zc);
+            const lr r = nb_ratio(f, ddx, ddy, ddu, ddv, zl);
             if (k == 0) r1 = r;
             else r2 = r;
           }
           // limiter and edge coefficient (hydro_kn_edgeviscosity.f90:185-214)
-          double cq, rs;
+          lr cq, rs;
           if (qf >= 0) {
             cq = s_f0[9][qf];
             rs = s_f0[10][qf];
           } else {
             const int ins = nb[is];
-            cq = C.cvisc1 * SQRT(half(cs2i + F.cs2[ins])) + C.cvisc2 * f.lu;
-            rs = rho0 + F.rho[ins];
+            cq = (lr)C.cvisc1 * SQRT((lr)half(cs2i + F.cs2[ins])) + (lr)C.cvisc2 * f.lu;
+            rs = (lr)(rho0 + F.rho[ins]);
           }
-          double w2 = minF(minF(minF(half(r1 + r2), twice(r1)), twice(r2)), 1.0);
-          w2 = maxF(0.0, w2);
-          const double edv = half(1.0 - w2) * rs * cq;
+          lr w2 = minF(minF(minF(half(r1 + r2), twice(r1)), twice(r2)), (lr)1);
+          w2 = maxF((lr)0, w2);
+          const lr edv = half((lr)1 - w2) * rs * cq;
           vmax = maxF_nn(vmax, edv * f.lu);  // never negative
           // edge force (hydro_kn_edgeviscosity.f90:219-282): the reference
           // normalises the midpoint-to-centroid vector c, orients it by the
           // sign of its product with the face vector and scales it back by
           // |c|: (exh, eyh) = -+(cy, -cx), the sign bit of w33 = cy*xh -
           // cx*yh choosing; |c| only enters the cut test
-          const double cx = is == 0 ? ga3 : (is == 1 ? negF(ga1) : (is == 2 ? negF(ga3) : ga1));
-          const double cy = is == 0 ? gb3 : (is == 1 ? negF(gb1) : (is == 2 ? negF(gb3) : gb1));
-          const double w33 = cy * f.xh - cx * f.yh;
-          const long long sb = bits64(w33) & (long long)0x8000000000000000ull;
-          const double exh = from_bits64(bits64(cy) ^ (long long)0x8000000000000000ull ^ sb);
-          const double eyh = from_bits64(bits64(cx) ^ sb);
-          const double w7sq = (is & 1) ? c1sq : c3sq;
-          const double w6b = f.du * exh + f.dv * eyh;
-          const double d = edv * DIV(w6b, maxF_nn(f.lu, zc));
+          const lr cx = is == 0 ? ga3 : (is == 1 ? negF(ga1) : (is == 2 ? negF(ga3) : ga1));
+          const lr cy = is == 0 ? gb3 : (is == 1 ? negF(gb1) : (is == 2 ? negF(gb3) : gb1));
+          const lr w33 = cy * f.xh - cx * f.yh;
+          const lr exh = negxorsign(cy, w33);
+          const lr eyh = xorsign(cx, w33);
+          const lr w7sq = (is & 1) ? c1sq : c3sq;
+          const lr w6b = f.du * exh + f.dv * eyh;
+          const lr d = edv * DIV(w6b, maxF_nn(f.lu, zl));
           edx[is] = f.du * d;
           edy[is] = f.dv * d;
-          if (le_nn(f.lu, zc) || geF(zc, w6b) || le_nn(w7sq, zc * zc) || le_nn(f.lx, zc)) {
-            edx[is] = 0.0;
-            edy[is] = 0.0;
+          if (le_nn(f.lu, zl) || geF(zl, w6b) || le_nn(w7sq, zl * zl) || le_nn(f.lx, zl)) {
+            edx[is] = (lr)0;
+            edy[is] = (lr)0;
           }
         }
       }
-      visc = vmax * DIV(2.0, maxF(rho0, zc));
+      visc = (double)(vmax * DIV((lr)2, maxF((lr)rho0, zl)));
       F.cnviscx[iel] = make_d4(edx[0] - edx[3], edx[1] - edx[0], edx[2] - edx[1], edx[3] - edx[2]);
       F.cnviscy[iel] = make_d4(edy[0] - edy[3], edy[1] - edy[0], edy[2] - edy[1], edy[3] - edy[2]);
       F.visc[iel] = visc;

@@ -2,7 +2,7 @@
 // the C++ counterpart of the reference's executable for the hot path
 // (inf_control_main.f90: init, the solver loop, short prints, validation).
 //
-//   bookleaf_gb300 [--fp fast|exact] [--calls] [--max-steps N]
+//   bookleaf_gb300 [--fp fast|exact|mixed] [--calls] [--max-steps N]
 //                  [--print-every N] [--dump-setup FILE] [--dump-final FILE]
 //                  CONTROL_FILE
 //
@@ -24,7 +24,7 @@ namespace {
 
 void usage() {
   std::fprintf(stderr,
-               "usage: bookleaf_gb300 [--fp fast|exact] [--calls] [--max-steps N]\n"
+               "usage: bookleaf_gb300 [--fp fast|exact|mixed] [--calls] [--max-steps N]\n"
                "                      [--print-every N] [--dump-setup FILE] [--dump-final FILE]\n"
                "                      CONTROL_FILE\n");
 }
@@ -56,6 +56,7 @@ int main(int argc, char** argv) {
       const std::string m = next();
       if (m == "fast") fp = BL_FP_FAST;
       else if (m == "exact") fp = BL_FP_EXACT;
+      else if (m == "mixed") fp = BL_FP_MIXED;
       else {
         usage();
         return 2;

@@ -126,8 +126,14 @@ typedef struct {
  * reference's order without fused multiply-add, which reproduces a
  * -ffp-contract=off CPU build bit for bit.  BL_FP_FAST lets the compiler
  * contract a*b+c into one FMA (gfortran does the same at -O2 on aarch64);
- * results then differ from the CPU build in the last bits. */
-enum { BL_FP_FAST = 0, BL_FP_EXACT = 1 };
+ * results then differ from the CPU build in the last bits.  BL_FP_MIXED
+ * (no counterpart in the reference: the demoted form for batches) is
+ * BL_FP_FAST with the edge viscosity's limiter ratios, edge coefficients
+ * and edge forces, the CFL lengths and divergence, and the remap limiters'
+ * gradients in FP32; positions, geometry and volumes, pressure forces,
+ * the energy update, the remap fluxes and the dt reduction stay FP64.
+ * Other values are rejected. */
+enum { BL_FP_FAST = 0, BL_FP_EXACT = 1, BL_FP_MIXED = 2 };
 
 typedef struct bl_ctx bl_ctx;
 
