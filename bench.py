@@ -249,17 +249,24 @@ def cpu_baseline(deck, nel, target_s=12.0, cores=1, steps=0, warmup=1):
 def run_ensemble(args, torch):
     """The batched ensemble (--workload ensemble; --size = number of meshes,
     default 512): every mesh of configs.ensemble advanced together by
-    bl_run_batch against the same meshes run one after another through the
-    plain per-mesh device loop (bl_run); both time K steps from t = 0 with
-    CUDA events on their stream, after W warm-up steps and a re-upload of
-    the initial state."""
+    bl_run_batch, in the floating-point mode --fp selects (mixed: the
+    demoted form), against the same meshes run one after another through
+    the plain per-mesh device loop (bl_run) in FP64 (fast; exact if --fp
+    exact).  Both run every mesh from t = 0 to its own end time (--steps K
+    > 0: K steps instead), timed with CUDA events, after W warm-up steps and
+    a re-upload of the initial state; the batch runs in chunks of 256 steps
+    and is set up again from the meshes still running whenever they hold
+    less than half its elements (BatchSolver.run_compacting).  The batch's
+    L1 errors against the FP64 per-mesh results are reported per mesh at
+    the end time and after 50 steps of both (the same step count)."""
     from bookleaf_f90_gb300 import BatchSolver, Problem, Solver, abi, configs
     import ctypes as ct
     n = args.size or 512
     seed = 20240607
-    K = args.steps if args.steps > 0 else 100
+    K = args.steps if args.steps > 0 else 10**9
     W = max(1, args.warmup)
     fp = {"exact": abi.FP_EXACT, "fast": abi.FP_FAST, "mixed": abi.FP_MIXED}[args.fp]
+    fp_plain = abi.FP_EXACT if args.fp == "exact" else abi.FP_FAST
     items = configs.ensemble(n, seed=seed)
     t0 = time.perf_counter()
     probs = [Problem.from_deck(d) for d, _ in items]
@@ -272,6 +279,41 @@ def run_ensemble(args, torch):
             np.copyto(p.fields[fid], a)
         ct.memmove(ct.addressof(p.timestep), ct.addressof(init[i][1]), ct.sizeof(abi.Timestep))
 
+    def l1s(pa, pb):
+        out = []
+        for f in (abi.ELDENSITY, abi.ELENERGY):
+            a, b = pa.fields[f], pb.fields[f]
+            out.append(float(np.sum(np.abs(a - b)) / max(np.sum(np.abs(b)), 1e-300)))
+        du = (np.abs(pa.fields[abi.NDU] - pb.fields[abi.NDU])
+              + np.abs(pa.fields[abi.NDV] - pb.fields[abi.NDV]))
+        un = np.abs(pb.fields[abi.NDU]) + np.abs(pb.fields[abi.NDV])
+        out.append(float(np.sum(du) / max(np.sum(un), 1e-300)))
+        return out
+
+    def l1_summary(rows):
+        a = np.array(rows)
+        names = ("density", "energy", "velocity")
+        return {nm: {"max": float(a[:, k].max()), "median": float(np.median(a[:, k]))}
+                for k, nm in enumerate(names)}
+
+    # ---- L1 after 50 steps: the batch in its mode against the batch in
+    # FP64 (equal, mesh by mesh, to each mesh alone: tests/test_gpu_batch.py)
+    l1_50 = None
+    if fp != fp_plain:
+        ref = [p.copy() for p in probs]
+        bm = BatchSolver(probs, fp_mode=fp)
+        assert bm.run(max_steps=50)[0] == 0, bm.error.message
+        bm.sync_to_host(0)
+        bm.close()
+        bf = BatchSolver(ref, fp_mode=fp_plain)
+        assert bf.run(max_steps=50)[0] == 0, bf.error.message
+        bf.sync_to_host(0)
+        bf.close()
+        l1_50 = l1_summary([l1s(a, b) for a, b in zip(probs, ref)])
+        del ref
+        for i, p in enumerate(probs):
+            restore(p, i)
+
     # ---- batched: autotune (steps per graph, node block size), warm up
     b = BatchSolver(probs, fp_mode=fp)
     tg, tb, tms = b.autotune()
@@ -282,40 +324,45 @@ def run_ensemble(args, torch):
     b.sync_to_device(0)
     stream = torch.cuda.ExternalStream(b.stream)
     n0 = [p.timestep.nstep for p in probs]
-    l0 = b.kernel_launches
+    l0 = b.total_launches
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     with ClockSampler(torch.cuda.current_device()) as clk:
         e0.record(stream)
-        ierr, status, nsteps = b.run(max_steps=K)
-        e1.record(stream)
+        ierr, status, nsteps = b.run_compacting(max_steps=K)
+        e1.record(torch.cuda.ExternalStream(b.stream))
         e1.synchronize()
     assert ierr == 0, b.error.message
     ms_b = e0.elapsed_time(e1)
-    zc_b = sum(nel * (p.timestep.nstep - s0) for nel, p, s0 in zip(nels, probs, n0))
-    active = sum(1 for p, s0 in zip(probs, n0) if p.timestep.nstep - s0 == nsteps)
-    launches = b.kernel_launches - l0
+    steps_b = [p.timestep.nstep - s0 for p, s0 in zip(probs, n0)]
+    zc_b = sum(nel * k for nel, k in zip(nels, steps_b))
+    done = sum(1 for p in probs if p.timestep.time >= p.config.time_end)
+    launches = b.total_launches - l0
+    compactions = list(b.compactions)
+    b.sync_to_host(0)
     b.close()
+    batch_final = [p.copy() for p in probs]
     value = zc_b / (ms_b * 1e-3)
-    # ---- e2e: batch set-up from the host arrays, K steps, full download
+    # ---- e2e: batch set-up from the host arrays, the same run, full download
     for i, p in enumerate(probs):
         restore(p, i)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     be = BatchSolver(probs, fp_mode=fp)
-    ierr, _, ne = be.run(max_steps=K)
+    ierr, _, ne = be.run_compacting(max_steps=K)
     be.sync_to_host(0)
     t1 = time.perf_counter()
     assert ierr == 0, be.error.message
     zc_e = sum(nel * p.timestep.nstep for nel, p in zip(nels, probs))
     h2d = sum(a.nbytes for p in probs for a in p.fields.values())
     be.close()
-    # ---- plain: each mesh alone
+    # ---- plain: each mesh alone in FP64
     ms_p, zc_p = 0.0, 0
+    rows_end, dt_end = [], []
     for i, p in enumerate(probs):
         restore(p, i)
-        s = Solver(p, fp_mode=fp)
+        s = Solver(p, fp_mode=fp_plain)
         ierr, _ = s.run(max_steps=W, ts=p.timestep.copy(), history=False)
         assert ierr == 0, s.error.message
         restore(p, i)
@@ -331,27 +378,46 @@ def run_ensemble(args, torch):
         assert ierr == 0, s.error.message
         ms_p += q0.elapsed_time(q1)
         zc_p += p.nel * (ts.nstep - init[i][1].nstep)
+        s.sync_to_host(0)
+        p.timestep = ts
+        rows_end.append(l1s(batch_final[i], p))
+        dt_end.append(abs(batch_final[i].timestep.time - ts.time) / max(ts.dt, 1e-300))
         s.close()
     plain = zc_p / (ms_p * 1e-3)
     hbm_peak, peak_kind = load_peaks()
     achieved = value * B_EUL / 1e9
-    return {"metric": METRIC, "what": "batched ensemble vs the plain per-mesh GPU path",
+    return {"metric": METRIC, "what": "batched ensemble vs the plain per-mesh FP64 GPU path",
             "value": value, "unit": "zone-cycles/s", "n_gpus": 1, "steps": nsteps,
             "warmup": W, "ms_per_step": ms_b / max(1, nsteps), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if fp != abi.FP_MIXED else "f64+f32 (mixed)", "data": "synthetic",
             "config": {"workload": "ensemble_%d_eulerian_sod_sedov" % n, "instances": n,
                        "seed": seed, "nel_total": sum(nels), "nel_min": min(nels),
                        "nel_max": max(nels), "fp_mode": args.fp,
-                       "meshes_active_whole_window": active,
-                       "timed": "%d steps from t=0" % nsteps,
-                       "loop": "bl_run_batch, CUDA graphs of %d steps" % tg,
+                       "meshes_at_end_time": done,
+                       "timed": ("every mesh from t=0 to its own end time (%d to %d steps)"
+                                 % (min(steps_b), max(steps_b))) if K >= 10**9 else
+                                "%d steps from t=0" % nsteps,
+                       "loop": "bl_run_batch, CUDA graphs of %d steps, in chunks of 256 "
+                               "steps; the batch is set up again from the meshes still "
+                               "running when they hold less than half its elements "
+                               "(BatchSolver.run_compacting)" % tg,
+                       "compactions": [{"after_step": a, "meshes": m, "elements": e}
+                                       for a, m, e in compactions],
                        "autotune": {"graph_steps": tg, "node_block": tb,
                                     "ms_per_step": {"%d,%d" % k: v for k, v in tms.items()}},
                        "setup_s": setup_s},
             "plain_per_mesh": {"value": plain, "unit": "zone-cycles/s", "ms_total": ms_p,
-                               "how": "each mesh alone through bl_run, the same %d steps "
-                                      "from t=0, CUDA events, times summed" % K},
+                               "fp_mode": "exact" if fp_plain == abi.FP_EXACT else "fast",
+                               "how": "each mesh alone through bl_run in FP64, the same run "
+                                      "from t=0, CUDA events, times summed"},
             "batched_over_plain": value / plain,
+            "l1_vs_plain_fp64": {"at_end_time": l1_summary(rows_end),
+                                 "end_time_offset_in_dt_max": float(max(dt_end)),
+                                 "after_50_steps": l1_50,
+                                 "how": "per mesh: sum|batch - plain| / sum|plain| of density, "
+                                        "specific energy and the velocity field; max and "
+                                        "median over the meshes"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": None,
                          "peak_kind": peak_kind,

@@ -18,7 +18,13 @@ from .solver import SolverError
 class BatchSolver:
     def __init__(self, problems, fp_mode=abi.FP_FAST):
         self.L = load()
-        self.problems = list(problems)
+        self.fp_mode = fp_mode
+        self.launches_closed = 0     # kernel launches of contexts replaced by compaction
+        self.compactions = []        # (step, meshes, elements) of each rebuild
+        self._init(list(problems))
+
+    def _init(self, problems):
+        self.problems = problems
         n = len(self.problems)
         self.error = abi.Error()
         self._tabs = [p.pointer_table() for p in self.problems]
@@ -28,7 +34,7 @@ class BatchSolver:
         self.ctx = ct.c_void_p()
         ierr = self.L.bl_init_batch(ct.byref(self.ctx), n, ct.cast(self._sizes, ct.c_void_p),
                                     ct.cast(self._configs, ct.c_void_p),
-                                    ct.cast(self._dh, ct.c_void_p), int(fp_mode),
+                                    ct.cast(self._dh, ct.c_void_p), int(self.fp_mode),
                                     ct.byref(self.error))
         if ierr != 0:
             raise SolverError(ierr, self.error.iout, self.error.message)
@@ -50,6 +56,44 @@ class BatchSolver:
         for p, t in zip(self.problems, ts):
             ct.memmove(ct.addressof(p.timestep), ct.addressof(t), ct.sizeof(abi.Timestep))
         return ierr, list(status), nsteps.value
+
+    def run_compacting(self, max_steps=10**9, keep=0.5, chunk=256):
+        """run() in chunks of `chunk` steps that drops finished meshes: when
+        the meshes still running (before their end time, no error) hold
+        fewer than `keep` of the batch's elements, their state is brought to
+        the host (their own Problem arrays) and the batch is set up again
+        from them alone, so that the kernels no longer launch over finished
+        meshes.  Every mesh still ends as it would alone: its state passes
+        through the host unchanged and the kernels are the same.  Returns
+        (ierr, {id(problem): status}, steps run)."""
+        everyone = list(self.problems)
+        status = {id(p): 0 for p in everyone}
+        done = 0
+        ierr = 0
+        while done < max_steps:
+            ierr, st, n = self.run(max_steps=min(chunk, max_steps - done))
+            for p, v in zip(self.problems, st):
+                status[id(p)] = v
+            done += n
+            if ierr != 0 or n == 0:
+                break
+            alive = [p for p, v in zip(self.problems, st)
+                     if v == 0 and p.timestep.time < p.config.time_end]
+            if not alive:
+                break
+            nel_all = sum(p.nel for p in self.problems)
+            nel_alive = sum(p.nel for p in alive)
+            if nel_alive < keep * nel_all:
+                self.sync_to_host(0)
+                self.launches_closed += self.kernel_launches
+                self.close()
+                self.compactions.append((done, len(alive), nel_alive))
+                self._init(alive)
+        return ierr, status, done
+
+    @property
+    def total_launches(self):
+        return self.launches_closed + self.kernel_launches
 
     def autotune(self):
         """Chooses the steps per graph and the node kernels' block size by

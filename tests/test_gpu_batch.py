@@ -60,6 +60,27 @@ def test_batch_equals_each_mesh_alone(decks, fp):
     b.close()
 
 
+@pytest.mark.parametrize("decks", [LAGRANGIAN, EULERIAN], ids=["lagrangian", "eulerian"])
+def test_compacting_run_equals_each_mesh_alone(decks):
+    """run_compacting rebuilds the batch from the meshes still running
+    (their state through the host) whenever they hold less than `keep` of
+    the elements; with chunks of 8 steps and keep 0.9 it rebuilds several
+    times, and every mesh still ends bit for bit as alone."""
+    probs = [Problem.from_deck(d) for d in decks]
+    b = BatchSolver(probs, fp_mode=abi.FP_EXACT)
+    ierr, status, nsteps = b.run_compacting(keep=0.9, chunk=8)
+    assert ierr == 0 and all(v == 0 for v in status.values()), b.error.message
+    b.sync_to_host(0)
+    assert len(b.compactions) >= 1
+    assert b.total_launches > 0
+    b.close()
+    for d, p in zip(decks, probs):
+        ierr1, q = _alone(d, abi.FP_EXACT)
+        assert ierr1 == 0
+        assert _same_timestep(p.timestep, q.timestep), (p.timestep.as_tuple(), q.timestep.as_tuple())
+        assert not compare(p, q, exact=True)
+
+
 def test_batch_step_limit_then_resume():
     """A run stopped after k steps and resumed ends where one run ends."""
     probs = [Problem.from_deck(d) for d in LAGRANGIAN]
