@@ -5,7 +5,9 @@ Eight translation units, compiled in parallel with nvcc:
                  -DBL_FAST_ALGEBRA=1          algebraic identities allowed)
   bl_kernels.cu  -DBL_NS=exact --fmad=false  (bit-reproducible path)
   bl_kernels.cu  -DBL_NS=mixed --fmad=true   (the fast build with the limiter
-                 -DBL_MIXED=1                 arithmetic in FP32)
+                 -DBL_MIXED=1                 arithmetic in FP32; FP32 divide and
+                 -prec-div/-prec-sqrt=false   square root approximate, FP32
+                 -ftz=true                    subnormals flushed: FP64 untouched)
   bl_capi.cu                                  (the C-ABI, host code)
   bl_noalloc.cu  --fmad=false                 (allocation-free getdt: the exact
                                               build's k_getdt)
@@ -66,7 +68,8 @@ def build(force=False, verbose=False, extra=()):
                    "-o", os.path.join(BUILD, "k_fast.o")]),
         (common + ["--fmad=false", "-DBL_NS=exact", "-c", os.path.join(CSRC, "bl_kernels.cu"),
                    "-o", os.path.join(BUILD, "k_exact.o")]),
-        (common + ["--fmad=true", "-DBL_NS=mixed", "-DBL_FAST_ALGEBRA=1", "-DBL_MIXED=1", "-c",
+        (common + ["--fmad=true", "-DBL_NS=mixed", "-DBL_FAST_ALGEBRA=1", "-DBL_MIXED=1",
+                   "-ftz=true", "-prec-div=false", "-prec-sqrt=false", "-c",
                    os.path.join(CSRC, "bl_kernels.cu"), "-o", os.path.join(BUILD, "k_mixed.o")]),
         (common + ["-c", os.path.join(CSRC, "bl_capi.cu"), "-o", os.path.join(BUILD, "capi.o")]),
         (common + ["--fmad=false", "-c", os.path.join(CSRC, "bl_noalloc.cu"),

@@ -78,24 +78,19 @@ __device__ __forceinline__ bool prod_le0(double w1, double w2) {
 // (mA mB (mA + mB)) and |grad| = min(|w8|, |A|/mA, |B|/mB), zero unless A
 // and B have the same sign, with the sign of S.  The operands are brought
 // into FP32's range by powers of two taken from their exponents (exact),
-// and the result scaled back in FP64.
+// and the result scaled back, all on the integer pipe (f32_of, f64_of).
 __device__ __forceinline__ int exp_of(double x) {
   return (int)((bits64(x) >> 52) & 0x7ff) - 1023;
-}
-__device__ __forceinline__ double pow2c(int k) {  // 2^k, k clamped to the normal range
-  k = k < -1022 ? -1022 : (k > 1023 ? 1023 : k);
-  return from_bits64((long long)(k + 1023) << 52);
 }
 __device__ __forceinline__ double grad_f32(double A, double B, double mA, double mB, double S) {
   if (prod_le0(A, B)) return 0.0;
   const int ev = exp_of(maxF_nn(absF(A), absF(B)));
   const int em = exp_of(maxF_nn(mA, mB));
-  const double sv = pow2c(-ev), sm = pow2c(-em);
-  const float a = (float)(A * sv), b = (float)(B * sv);
-  const float ma = (float)(mA * sm), mb = (float)(mB * sm);
+  const float a = f32_of(A, -ev), b = f32_of(B, -ev);
+  const float ma = f32_of(mA, -em), mb = f32_of(mB, -em);
   const float w8 = (a * mb * mb + b * ma * ma) / (ma * mb * (ma + mb));
   const float g = fminf(fminf(fabsf(w8), fabsf(a) / ma), fabsf(b) / mb);
-  return signF((double)g * pow2c(ev) * pow2c(-em), S);
+  return signF(f64_of(g, ev - em), S);
 }
 #endif
 

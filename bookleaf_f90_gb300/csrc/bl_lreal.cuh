@@ -67,6 +67,48 @@ __device__ __forceinline__ float negxorsign(float a, float s) {
   return __int_as_float(__float_as_int(a) ^ 0x80000000 ^ (__float_as_int(s) & 0x80000000));
 }
 
+// FP64 <-> FP32 on the integer pipe, with a power-of-two scaling folded
+// into the exponent: f32_of(x, k) is x * 2^k truncated to FP32 (its
+// leading 24 significant bits), zero where that falls below FP32's normal
+// range and infinite above it; f64_of(f, k) is f * 2^k exactly for a
+// normal f (zero for zero or subnormal f).  The FP64 unit, 1/64 of the
+// FP32 rate on GB300, is not used.
+__device__ __forceinline__ float f32_of(double x, int k) {
+  const long long b = bits64(x);
+  const unsigned sign = (unsigned)((unsigned long long)b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7ff);
+  const int fe = e - 1023 + 127 + k;
+  const unsigned m = (unsigned)((unsigned long long)b >> 29) & 0x7fffffu;
+  if (e == 0 || fe <= 0) return __int_as_float((int)sign);
+  if (fe >= 255) return __int_as_float((int)(sign | 0x7f800000u));
+  return __int_as_float((int)(sign | ((unsigned)fe << 23) | m));
+}
+__device__ __forceinline__ double f64_of(float f, int k) {
+  const unsigned b = (unsigned)__float_as_int(f);
+  const long long sign = (long long)(b & 0x80000000u) << 32;
+  const int fe = (int)((b >> 23) & 0xff);
+  if (fe == 0) return from_bits64(sign);
+  int e = fe == 255 ? 0x7ff : fe - 127 + 1023 + k;
+  if (fe != 255 && e <= 0) return from_bits64(sign);
+  if (fe != 255 && e >= 0x7ff) return from_bits64(sign | 0x7ff0000000000000ll);
+  return from_bits64(sign | ((long long)e << 52) | ((long long)(b & 0x7fffffu) << 29));
+}
+// an FP64 value as an lr (FP32: f32_of), and back
+__device__ __forceinline__ lr to_lr(double x) {
+#if BL_MIXED
+  return f32_of(x, 0);
+#else
+  return x;
+#endif
+}
+__device__ __forceinline__ double from_lr(lr x) {
+#if BL_MIXED
+  return f64_of(x, 0);
+#else
+  return x;
+#endif
+}
+
 // the cut-off zerocut as an lr: FP32 has no 1e-40, so the smallest
 // normal FP32 stands in for cut-offs below it
 __device__ __forceinline__ lr lr_cut(double zc) {

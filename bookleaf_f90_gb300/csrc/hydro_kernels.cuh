@@ -562,9 +562,9 @@ __device__ __forceinline__ double getdt_cfl_len(const DevFields& F, const DevCfg
 #if BL_FAST_ALGEBRA
   return __ldg(C.zmidlength + ireg)
              ? min_dlm(x, y)
-             : (double)min_dln_iso<lr>(x, y, lr_cut(C.zcut), (lr)F.a1[iel], (lr)F.a2[iel],
-                                       (lr)F.a3[iel], (lr)F.b1[iel], (lr)F.b2[iel],
-                                       (lr)F.b3[iel]);
+             : from_lr(min_dln_iso<lr>(x, y, lr_cut(C.zcut), to_lr(F.a1[iel]), to_lr(F.a2[iel]),
+                                       to_lr(F.a3[iel]), to_lr(F.b1[iel]), to_lr(F.b2[iel]),
+                                       to_lr(F.b3[iel])));
 #else
   return __ldg(C.zmidlength + ireg) ? min_dlm(x, y) : min_dln(x, y, C.zcut);
 #endif
@@ -574,11 +574,11 @@ __device__ __forceinline__ double getdt_cfl_len(const DevFields& F, const DevCfg
 __device__ __forceinline__ void getdt_div(const DevFields& F, int iel, const double* u,
                                           const double* v, double& divv, int& divi) {
 #if BL_MIXED
-  const lr A1 = (lr)F.a1[iel], A3 = (lr)F.a3[iel], B1 = (lr)F.b1[iel], B3 = (lr)F.b3[iel];
-  lr wl = (lr)u[0] * (-B3 + B1) + (lr)v[0] * (A3 - A1) + (lr)u[1] * (B3 + B1) +
-          (lr)v[1] * (-A3 - A1) + (lr)u[2] * (B3 - B1) + (lr)v[2] * (-A3 + A1) +
-          (lr)u[3] * (-B3 - B1) + (lr)v[3] * (A3 + A1);
-  const double w1 = (double)DIV(absF(wl), (lr)F.vol[iel]);
+  const lr A1 = to_lr(F.a1[iel]), A3 = to_lr(F.a3[iel]), B1 = to_lr(F.b1[iel]), B3 = to_lr(F.b3[iel]);
+  lr wl = to_lr(u[0]) * (-B3 + B1) + to_lr(v[0]) * (A3 - A1) + to_lr(u[1]) * (B3 + B1) +
+          to_lr(v[1]) * (-A3 - A1) + to_lr(u[2]) * (B3 - B1) + to_lr(v[2]) * (-A3 + A1) +
+          to_lr(u[3]) * (-B3 - B1) + to_lr(v[3]) * (A3 + A1);
+  const double w1 = from_lr(DIV(absF(wl), to_lr(F.vol[iel])));
 #else
   const double A1 = F.a1[iel], A3 = F.a3[iel], B1 = F.b1[iel], B3 = F.b3[iel];
   double w1 = u[0] * (-B3 + B1) + v[0] * (A3 - A1) + u[1] * (B3 + B1) + v[1] * (-A3 - A1) +
@@ -606,7 +606,7 @@ __device__ __forceinline__ void getdt_cfl(const DevFields& F, int iel, double le
   }
   F.cs2v[iel] = cs2v;
 #if BL_MIXED
-  const double r11 = len < 0.0 ? DBL_MAX : (double)DIV((lr)len, (lr)cs2v);
+  const double r11 = len < 0.0 ? DBL_MAX : from_lr(DIV(to_lr(len), to_lr(cs2v)));
 #else
   const double r11 = len < 0.0 ? DBL_MAX : DIV(len, cs2v);
 #endif
@@ -896,8 +896,8 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
   }
   if (!C.ztq) {
     if (inmesh) {
-      const FaceQ f0 = face_q((lr)(u[1] - u[0]), (lr)(v[1] - v[0]), (lr)(x[1] - x[0]),
-                              (lr)(y[1] - y[0]), zl);
+      const FaceQ f0 = face_q(to_lr(u[1] - u[0]), to_lr(v[1] - v[0]), to_lr(x[1] - x[0]),
+                              to_lr(y[1] - y[0]), zl);
       s_f0[0][t] = f0.du;
       s_f0[1][t] = f0.dv;
       s_f0[2][t] = f0.lu;
@@ -908,16 +908,16 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
       s_f0[7][t] = f0.yh;
       s_f0[8][t] = f0.w1;
       const int nb0 = __ldg(F.ielel + iel).x;
-      s_f0[9][t] = (lr)C.cvisc1 * SQRT((lr)half(F.cs2[iel] + F.cs2[nb0])) + (lr)C.cvisc2 * f0.lu;
-      s_f0[10][t] = (lr)(F.rho[iel] + F.rho[nb0]);
-      s_fd[0][t] = x[2] - x[1];
-      s_fd[1][t] = y[2] - y[1];
-      s_fd[2][t] = u[2] - u[1];
-      s_fd[3][t] = v[2] - v[1];
-      s_fd[4][t] = x[0] - x[3];
-      s_fd[5][t] = y[0] - y[3];
-      s_fd[6][t] = u[0] - u[3];
-      s_fd[7][t] = v[0] - v[3];
+      s_f0[9][t] = to_lr(C.cvisc1) * SQRT(to_lr(half(F.cs2[iel] + F.cs2[nb0]))) + to_lr(C.cvisc2) * f0.lu;
+      s_f0[10][t] = to_lr(F.rho[iel] + F.rho[nb0]);
+      s_fd[0][t] = to_lr(x[2] - x[1]);
+      s_fd[1][t] = to_lr(y[2] - y[1]);
+      s_fd[2][t] = to_lr(u[2] - u[1]);
+      s_fd[3][t] = to_lr(v[2] - v[1]);
+      s_fd[4][t] = to_lr(x[0] - x[3]);
+      s_fd[5][t] = to_lr(y[0] - y[3]);
+      s_fd[6][t] = to_lr(u[0] - u[3]);
+      s_fd[7][t] = to_lr(v[0] - v[3]);
     }
     __syncthreads();
   }
@@ -935,7 +935,7 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
       // the vector from an edge's midpoint to the centroid is (a3,b3),
       // (-a1,-b1), (-a3,-b3), (a1,b1) for faces 0..3 (corners written as
       // s -+ a1 +- a2 -+ a3, exact in real arithmetic)
-      const lr ga1 = (lr)F.a1[iel], ga3 = (lr)F.a3[iel], gb1 = (lr)F.b1[iel], gb3 = (lr)F.b3[iel];
+      const lr ga1 = to_lr(F.a1[iel]), ga3 = to_lr(F.a3[iel]), gb1 = to_lr(F.b1[iel]), gb3 = to_lr(F.b3[iel]);
       // |c|^2 of faces 1,3 and of faces 0,2 (only the cut test uses it)
       const lr c1sq = ga1 * ga1 + gb1 * gb1, c3sq = ga3 * ga3 + gb3 * gb3;
       // max over faces of edv * |du|; the reference's max of
@@ -985,8 +985,8 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
               f.yh = negF(s_f0[7][q]);
               f.w1 = s_f0[8][q];
             } else {
-              f = face_q((lr)(u[3] - u[2]), (lr)(v[3] - v[2]), (lr)(x[3] - x[2]),
-                         (lr)(y[3] - y[2]), zl);
+              f = face_q(to_lr(u[3] - u[2]), to_lr(v[3] - v[2]), to_lr(x[3] - x[2]),
+                         to_lr(y[3] - y[2]), zl);
             }
           } else {
             const int o = is == 1 ? 0 : 4;
@@ -1014,10 +1014,10 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
               const int4 m = __ldg(F.ielnd + inb);
               const int mm[4] = {m.x, m.y, m.z, m.w};
               const int a = mm[ins], b = mm[(ins + 1) & 3];
-              ddx = F.ndx[b] - F.ndx[a];
-              ddy = F.ndy[b] - F.ndy[a];
-              ddu = F.ndu[b] - F.ndu[a];
-              ddv = F.ndv[b] - F.ndv[a];
+              ddx = to_lr(F.ndx[b] - F.ndx[a]);
+              ddy = to_lr(F.ndy[b] - F.ndy[a]);
+              ddu = to_lr(F.ndu[b] - F.ndu[a]);
+              ddv = to_lr(F.ndv[b] - F.ndv[a]);
             }
             const lr r = nb_ratio(f, ddx, ddy, ddu, ddv, zl);
             if (k == 0) r1 = r;
@@ -1030,8 +1030,8 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
             rs = s_f0[10][qf];
           } else {
             const int ins = nb[is];
-            cq = (lr)C.cvisc1 * SQRT((lr)half(cs2i + F.cs2[ins])) + (lr)C.cvisc2 * f.lu;
-            rs = (lr)(rho0 + F.rho[ins]);
+            cq = to_lr(C.cvisc1) * SQRT(to_lr(half(cs2i + F.cs2[ins]))) + to_lr(C.cvisc2) * f.lu;
+            rs = to_lr(rho0 + F.rho[ins]);
           }
           lr w2 = minF(minF(minF(half(r1 + r2), twice(r1)), twice(r2)), (lr)1);
           w2 = maxF((lr)0, w2);
@@ -1058,9 +1058,11 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
           }
         }
       }
-      visc = (double)(vmax * DIV((lr)2, maxF((lr)rho0, zl)));
-      F.cnviscx[iel] = make_d4(edx[0] - edx[3], edx[1] - edx[0], edx[2] - edx[1], edx[3] - edx[2]);
-      F.cnviscy[iel] = make_d4(edy[0] - edy[3], edy[1] - edy[0], edy[2] - edy[1], edy[3] - edy[2]);
+      visc = from_lr(vmax * DIV((lr)2, maxF(to_lr(rho0), zl)));
+      F.cnviscx[iel] = make_d4(from_lr(edx[0] - edx[3]), from_lr(edx[1] - edx[0]),
+                               from_lr(edx[2] - edx[1]), from_lr(edx[3] - edx[2]));
+      F.cnviscy[iel] = make_d4(from_lr(edy[0] - edy[3]), from_lr(edy[1] - edy[0]),
+                               from_lr(edy[2] - edy[1]), from_lr(edy[3] - edy[2]));
       F.visc[iel] = visc;
     } else {
       visc = F.visc[iel];

@@ -82,7 +82,7 @@ def test_mixed_against_fp64(name):
 def test_mixed_batch_equals_each_mesh_alone():
     decks = [configs.sod(20, 4, time_end=0.03, eulerian=True),
              configs.sedov(14, time_end=0.02, eulerian=True, gamma=1.6),
-             configs.sod(24, 4, time_end=0.05)]
+             configs.sod(24, 4, time_end=0.05, eulerian=True, pratio=100.0)]
     probs = [Problem.from_deck(d) for d in decks]
     b = BatchSolver(probs, fp_mode=abi.FP_MIXED)
     ierr, status, nsteps = b.run()
