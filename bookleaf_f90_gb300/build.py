@@ -34,7 +34,7 @@ OUTDIR = os.path.join(HERE, "_lib")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(OUTDIR, "libbookleaf_gb300.so")
 EXE = os.path.join(OUTDIR, "bookleaf_gb300")
-HOST_SOURCES = ("deck", "mesh", "ic", "problem", "solver", "main")
+HOST_SOURCES = ("deck", "mesh", "ic", "problem", "solver", "io", "main")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -102,6 +102,11 @@ std::string read_file(const std::string& path);
 // Set-up dump (tests compare it with the Python harness array by array).
 void write_setup_dump(const Problem& p, const std::string& path);
 
+// The reference's visualisation dump (io_dr_silo.f90:70-262) as a VTK
+// legacy unstructured grid: mesh, materials with volume fractions,
+// density, energy, pressure, region, node velocity (io.cpp).
+void write_vtk(const Problem& p, const std::string& path);
+
 // hydro_kn_calc_shortprint (hydro_kn_print.F90:52-101) per region or
 // material flag: volume, mass, internal and kinetic energy, mass-weighted
 // pressure, pressure and density extremes (and the averages of

@@ -4,12 +4,15 @@
 //
 //   bookleaf_gb300 [--fp fast|exact|mixed] [--calls] [--max-steps N]
 //                  [--print-every N] [--dump-setup FILE] [--dump-final FILE]
-//                  CONTROL_FILE
+//                  [--vtk FILE] [--vtk-setup FILE] CONTROL_FILE
 //
 // --calls runs the loop of inf_control_solver on the host, one call per
 // entry point per step, printing a step line like time_dr_utils.f90:47-50;
 // the default runs it on the device (bl_run).  --dump-setup writes the
-// initial state and exits without touching a GPU.  A control file whose
+// initial state and exits without touching a GPU.  --vtk writes the final
+// state as the reference's visualisation dump (io_dr_silo.f90, as VTK:
+// io.cpp); --vtk-setup writes the initial state so and exits without a
+// GPU.  A control file whose
 // name contains "sod" is validated with the reference's Sod check
 // (check_dr_validate.f90).
 #include <chrono>
@@ -26,7 +29,7 @@ void usage() {
   std::fprintf(stderr,
                "usage: bookleaf_gb300 [--fp fast|exact|mixed] [--calls] [--max-steps N]\n"
                "                      [--print-every N] [--dump-setup FILE] [--dump-final FILE]\n"
-               "                      CONTROL_FILE\n");
+               "                      [--vtk FILE] [--vtk-setup FILE] CONTROL_FILE\n");
 }
 
 std::string trimmed(const char* s, size_t n) {
@@ -42,7 +45,7 @@ int main(int argc, char** argv) {
   bool calls = false;
   long max_steps = 2147483647L;
   long print_every = 0;
-  std::string deck, dump_setup, dump_final;
+  std::string deck, dump_setup, dump_final, vtk, vtk_setup;
   for (int i = 1; i < argc; i++) {
     const std::string a = argv[i];
     auto next = [&]() -> std::string {
@@ -71,6 +74,10 @@ int main(int argc, char** argv) {
       dump_setup = next();
     } else if (a == "--dump-final") {
       dump_final = next();
+    } else if (a == "--vtk") {
+      vtk = next();
+    } else if (a == "--vtk-setup") {
+      vtk_setup = next();
     } else if (!a.empty() && a[0] == '-') {
       usage();
       return 2;
@@ -92,9 +99,15 @@ int main(int argc, char** argv) {
   std::printf(" BookLeaf GB300 (%s)\n control file: %s\n nel=%d nnd=%d nreg=%d nmat=%d ncp=%d\n",
               bl_version(), deck.c_str(), p.sizes.nel, p.sizes.nnd, p.sizes.nreg, p.sizes.nmat,
               p.sizes.ncp);
-  if (!dump_setup.empty()) {
-    blh::write_setup_dump(p, dump_setup);
-    std::printf(" initial state written to %s\n", dump_setup.c_str());
+  if (!dump_setup.empty() || !vtk_setup.empty()) {
+    if (!dump_setup.empty()) {
+      blh::write_setup_dump(p, dump_setup);
+      std::printf(" initial state written to %s\n", dump_setup.c_str());
+    }
+    if (!vtk_setup.empty()) {
+      blh::write_vtk(p, vtk_setup);
+      std::printf(" initial state dump written to %s\n", vtk_setup.c_str());
+    }
     return 0;
   }
   int rc = 0;
@@ -141,9 +154,11 @@ int main(int argc, char** argv) {
       s.check_sod(ts.time, l1d, l1e);
       std::printf(" VALIDATION\n  Sod shocktube test case\n   L1 norm. of density: %16.9e\n", l1d);
     }
-    if (!dump_final.empty()) {
-      s.sync_to_host(0);
-      blh::write_setup_dump(p, dump_final);
+    if (!dump_final.empty() || !vtk.empty()) s.sync_to_host(0);
+    if (!dump_final.empty()) blh::write_setup_dump(p, dump_final);
+    if (!vtk.empty()) {
+      blh::write_vtk(p, vtk);
+      std::printf(" dump written to %s\n", vtk.c_str());
     }
   } catch (const blh::SolverError& e) {
     std::fprintf(stderr, "%s\n", e.what());

@@ -61,3 +61,24 @@ def test_driver_sod_validation(tmp_path):
     ref = sod_l1(p, p.timestep.time)[0]
     assert abs(l1 - ref) <= 1e-9 * abs(ref), (l1, ref)
     assert 1e-3 < l1 < 2e-2
+
+
+def test_driver_vtk_dump_of_the_final_state(tmp_path):
+    """--vtk writes the reference's visualisation dump (as VTK) of the
+    state at the end of the run: the mesh and fields equal the Python path's
+    final state bit for bit in exact mode, mixed cells included."""
+    from vtk_read import read_vtk
+    deck = configs.sod_multimaterial(40, 6, time_end=2.0)
+    vtk = tmp_path / "final.vtk"
+    out, (sizes, config, ts, fields) = _driver(tmp_path, deck, "sod_mm_deck", "--fp", "exact",
+                                               "--vtk", str(vtk))
+    title, pts, cells, cd, pd = read_vtk(vtk)
+    p = _python_final(deck)
+    assert "nstep=%d" % p.timestep.nstep in title
+    assert np.array_equal(pts[:, 0], p.fields[abi.NDX])
+    assert np.array_equal(pts[:, 1], p.fields[abi.NDY])
+    assert np.array_equal(cd["density"], p.fields[abi.ELDENSITY])
+    assert np.array_equal(cd["pressure"], p.fields[abi.ELPRESSURE])
+    assert np.array_equal(pd["velocity"][:, 0], p.fields[abi.NDU])
+    vf = np.array([v for k, v in cd.items() if k.startswith("volume_fraction_")])
+    assert np.allclose(vf.sum(axis=0), 1.0, rtol=0, atol=1e-12)

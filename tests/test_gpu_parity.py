@@ -277,3 +277,22 @@ def test_host_edits_of_the_timestep_take_effect():
         assert (tg.nstep, tg.dt, tg.time) == (tc.nstep, tc.dt, tc.time)
     s.sync_to_host(0)
     assert not compare(pg, pc, exact=True)
+
+
+def test_sinusoidal_interface_halts_like_the_oracle():
+    """The literal sinusoidal two-material Sod under the plain closure
+    stops with dt < dt_min on the device at the same step and time as the
+    CPU restatement (exact mode), well before t = 0.2."""
+    from oracle.oracle import Oracle
+    dk, fr = configs.sod_interface(200, 20, time_end=0.2)
+    base = Problem.from_deck(dk, material_fraction=fr)
+    pg, pc = base.copy(), base.copy()
+    o = Oracle(pc)
+    ierr_c, n_c = o.run(pc.timestep, 10**6)
+    s = Solver(pg, fp_mode=abi.FP_EXACT)
+    ierr_g, hist = s.run()
+    assert ierr_c != 0 and ierr_g != 0
+    assert s.error.message == "ERROR: dt < dt_min" == o.err.message.strip()
+    assert pg.timestep.nstep == pc.timestep.nstep and pg.timestep.time == pc.timestep.time
+    assert pg.timestep.time < 0.1
+    s.close()

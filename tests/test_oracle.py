@@ -161,3 +161,19 @@ def test_other_eos_forms_conserve(form):
     assert abs(e1 - e0) <= 1e-12 * abs(e0) * n
     if form == "tait":
         assert np.any(p.fields[abi.ELPRESSURE] == -0.1)
+
+
+def test_plain_closure_halts_on_the_sinusoidal_interface():
+    """The two-material Sod with the sinusoidal interface (amplitude 0.02,
+    8 periods) cannot be run to t = 0.2 under the reference's plain
+    closure: its mixed cells get neither artificial viscosity nor
+    hourglass control, collapse, and the step ends with dt < dt_min
+    (HALT_ALL) at t ~ 0.05 on 200x20.  The learned closure's measurements
+    therefore use a tilted planar interface the plain closure survives."""
+    dk, fr = configs.sod_interface(200, 20, time_end=0.2)
+    p = Problem.from_deck(dk, material_fraction=fr)
+    assert p.sizes.nmx > 100
+    o = Oracle(p)
+    ierr, n = o.run(p.timestep, 10**6)
+    assert ierr != 0 and o.err.message.strip() == "ERROR: dt < dt_min"
+    assert p.timestep.time < 0.1
