@@ -1,7 +1,7 @@
 """Benchmark of the BookLeaf hydro hot path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                    [--workload sedov|noh|noh-eul|sod|ensemble|closure|closure-ensemble]
+                    [--workload sedov|noh|noh-polar|noh-eul|sod|ensemble|closure|closure-ensemble]
                     [--size S]
 
 A step is one pass of the hot path (getdt + lagstep, + alestep for Eulerian
@@ -81,6 +81,12 @@ def workload_deck(name, size):
                 "sedov_%dx%d_lagrangian_t1_hg0.01_sp0.1" % (n, n), False)
     if name == "noh":
         return configs.noh(size or 2048), "noh_%dx%d_lagrangian" % (size or 2048, size or 2048), False
+    if name == "noh-polar":
+        # the reference's own Noh mesh (input/noh_large: 1800 x 720 on the
+        # polar quarter annulus); --size sets the radial cells, 0.4x around
+        nr = size or 1800
+        return (configs.noh_polar(nr, max(1, (nr * 2) // 5)),
+                "noh_polar_%dx%d_lagrangian_t0.6" % (nr, max(1, (nr * 2) // 5)), False)
     if name == "noh-eul":
         return configs.noh(size or 2048, eulerian=True), "noh_%dx%d_eulerian" % (size or 2048, size or 2048), True
     if name == "sod":

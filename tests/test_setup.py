@@ -162,3 +162,16 @@ def test_sinusoidal_interface_fractions_are_exact_areas():
     assert abs(np.sum(vf * area) - 0.05) <= 1e-9
     assert p.sizes.nmx == int(np.sum((vf > 0) & (vf < 1))) > 20
     assert p.sizes.ncp == 2 * p.sizes.nmx
+
+
+def test_noh_polar_generator_is_the_reference_deck():
+    """configs.noh_polar(75, 30), the generator of the Noh benchmark on the
+    reference's polar mesh, sets up the reference's own input/noh_small
+    exactly (every field and the configuration)."""
+    import golden
+    a = Problem.from_deck(configs.noh_polar(75, 30))
+    b = Problem.from_deck(golden.deck_text("noh_small"))
+    assert bytes(a.config) == bytes(b.config)
+    assert set(a.fields) == set(b.fields)
+    for fid in b.fields:
+        assert np.array_equal(a.fields[fid], b.fields[fid]), abi.NAMES[fid]
