@@ -120,28 +120,32 @@ def grid_index(problem, nx, ny):
 def material_sums(problem, index, ncell):
     """Volume, mass and internal energy of materials 1 and 2 in each of
     ncell cells (elements mapped by index), from pure elements and
-    mixed-cell components alike; arrays of shape (ncell, 2)."""
+    mixed-cell components alike; arrays of shape (ncell, 2).  Each sum runs
+    over the elements (then the components) in their order (np.bincount
+    accumulates in input order, as np.add.at does, many times faster)."""
     f = problem.fields
     ielmat = f[abi.IELMAT]
-    V, M, E = (np.zeros((ncell, 2)) for _ in range(3))
     pure = ielmat > 0
     cell, mat = index[pure], ielmat[pure] - 1
     keep = mat < 2
-    cell, mat = cell[keep], mat[keep]
+    bins = [2 * cell[keep] + mat[keep]]
     el_m = f[abi.ELMASS][pure][keep]
-    np.add.at(V, (cell, mat), f[abi.ELVOLUME][pure][keep])
-    np.add.at(M, (cell, mat), el_m)
-    np.add.at(E, (cell, mat), el_m * f[abi.ELENERGY][pure][keep])
+    vols = [f[abi.ELVOLUME][pure][keep]]
+    mass = [el_m]
+    ener = [el_m * f[abi.ELENERGY][pure][keep]]
     if problem.sizes.ncp > 0:
         cp_el = np.repeat(f[abi.IMXEL][:problem.sizes.nmx] - 1, f[abi.IMXNCP][:problem.sizes.nmx])
         cmat = f[abi.ICPMAT][:len(cp_el)] - 1
         keep = cmat < 2
-        cell, mat = index[cp_el[keep]], cmat[keep]
+        bins.append(2 * index[cp_el[keep]] + cmat[keep])
         cm = f[abi.CPMASS][:len(cp_el)][keep]
-        np.add.at(V, (cell, mat), f[abi.CPVOLUME][:len(cp_el)][keep])
-        np.add.at(M, (cell, mat), cm)
-        np.add.at(E, (cell, mat), cm * f[abi.CPENERGY][:len(cp_el)][keep])
-    return V, M, E
+        vols.append(f[abi.CPVOLUME][:len(cp_el)][keep])
+        mass.append(cm)
+        ener.append(cm * f[abi.CPENERGY][:len(cp_el)][keep])
+    b = np.concatenate(bins)
+    out = [np.bincount(b, weights=np.concatenate(w), minlength=2 * ncell).reshape(ncell, 2)
+           for w in (vols, mass, ener)]
+    return out[0], out[1], out[2]
 
 
 def features(config, V, M, E, dvol, dt):
