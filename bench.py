@@ -488,7 +488,7 @@ def run_closure(args, torch):
     net, norm, losses = closure.train(X, D, epochs=100)
     t2 = time.perf_counter()
 
-    def timed(p, learned, limit, volume_only=False):
+    def timed(p, learned, limit, volume_only=False, may_fail=False):
         s = Solver(p, fp_mode=fp)
         if learned:
             s.set_closure(net, norm, volume_only=volume_only)
@@ -511,6 +511,11 @@ def run_closure(args, torch):
             ierr, _ = s.run(max_steps=limit, history=False, ts=ts)
             e1.record(stream)
             e1.synchronize()
+        if ierr != 0 and may_fail:
+            out = {"failed": s.error.message.strip(), "time": ts.time,
+                   "steps": ts.nstep - ts0.nstep}
+            s.close()
+            return out
         assert ierr == 0, s.error.message
         assert ts.time >= p.config.time_end, "no end in %d steps" % limit
         p.timestep = ts
@@ -547,24 +552,28 @@ def run_closure(args, torch):
     assert ierr_e == 0, se.error.message
     ne = pe.timestep.nstep
     se.close()
-    # the same interface refined (4x, or 2x where the 4x-refined plain run
-    # would stop with dt < dt_min, from 4800 cells across), plain: the
-    # sub-cell truth at the end
+    # the same interface refined (4x by default), plain: the sub-cell
+    # truth at the end.  The plain closure itself stops with dt < dt_min on
+    # this interface from about 3,200 cells across (its mixed cells get no
+    # artificial viscosity); the line then records where, and the errors
+    # against the truth are absent (the comparison with the plain closure
+    # at the workload's own size stands).
     t3 = time.perf_counter()
-    R = args.refine or (4 if 4 * nx < 4800 else 2)
+    R = args.refine or 4
     deck4, frac4 = _closure_case(CLOSURE_TEST, R * nx, R * ny)
     pf = Problem.from_deck(deck4, material_fraction=frac4)
     fsetup = time.perf_counter() - t3
     fidx = closure.grid_index(pf, nx, ny)
-    rf = timed(pf, False, 40000)
-    Vf, Mf, _ = closure.material_sums(pf, fidx, nx * ny)
-    err_p = closure.mixed_errors(pp, idx, (Vf, Mf), cells)
-    err_l = closure.mixed_errors(pl, idx, (Vf, Mf), cells)
-    err_v = closure.mixed_errors(pv, idx, (Vf, Mf), cells)
+    rf = timed(pf, False, 40000, may_fail=True)
     shift_v, l1m_v, l1a_v = closure.against_plain(pv, pp, idx, nx, ny)
     shift, l1_mixed, l1_all = closure.against_plain(pl, pp, idx, nx, ny)
-    cd_p = closure.cell_density_error(pp, idx, (Vf, Mf), cells)
-    cd_l = closure.cell_density_error(pl, idx, (Vf, Mf), cells)
+    if "failed" not in rf:
+        Vf, Mf, _ = closure.material_sums(pf, fidx, nx * ny)
+        err_p = closure.mixed_errors(pp, idx, (Vf, Mf), cells)
+        err_l = closure.mixed_errors(pl, idx, (Vf, Mf), cells)
+        err_v = closure.mixed_errors(pv, idx, (Vf, Mf), cells)
+        cd_p = closure.cell_density_error(pp, idx, (Vf, Mf), cells)
+        cd_l = closure.cell_density_error(pl, idx, (Vf, Mf), cells)
     # the literal sinusoidal case under the plain closure
     dk, fr = configs.sod_interface(nx, ny, time_end=0.2)
     pq = Problem.from_deck(dk, material_fraction=fr)
@@ -599,13 +608,16 @@ def run_closure(args, torch):
                                     "data_s": t1 - t0, "train_s": t2 - t1}},
             "plain_closure": {"value": rp["rate"], "unit": "zone-cycles/s", "ms": rp["ms"],
                               "steps": rp["steps"]},
-            "refined_plain": {"refinement": R, "nel": pf.nel, "ms": rf["ms"],
-                              "steps": rf["steps"],
-                              "value": rf["rate"], "setup_s": fsetup},
-            "speedup_vs_refined_plain": rf["ms"] / rl["ms"],
+            "refined_plain": ({"refinement": R, "nel": pf.nel, "ms": rf["ms"],
+                               "steps": rf["steps"], "value": rf["rate"], "setup_s": fsetup}
+                              if "failed" not in rf else
+                              {"refinement": R, "nel": pf.nel, "stopped": rf["failed"],
+                               "at_time": rf["time"], "after_steps": rf["steps"]}),
+            "speedup_vs_refined_plain": rf["ms"] / rl["ms"] if "failed" not in rf else None,
             "closure_cells": {"seen": rl["closure_cells"], "rejected": rl["closure_rejected"]},
             "volume_only": {"value": rv["rate"], "unit": "zone-cycles/s",
-                            "errors_vs_refined": dict(zip(names, err_v)),
+                            "errors_vs_refined": (dict(zip(names, err_v))
+                                                  if "failed" not in rf else None),
                             "against_plain": {"interface_shift_cells_max": shift_v,
                                               "mixed_cell_density_l1_rel": l1m_v,
                                               "all_cell_density_l1_rel": l1a_v},
@@ -614,10 +626,11 @@ def run_closure(args, torch):
                             "how": "the materials keep their specific energies: the flow "
                                    "stays the plain closure's, the split between the "
                                    "materials is learned"},
-            "errors_vs_refined": {"plain": dict(zip(names, err_p), cell_density_rel_l1=cd_p),
-                                  "learned": dict(zip(names, err_l), cell_density_rel_l1=cd_l),
-                                  "how": "mean over the mixed cells at t = 0.2 against the "
-                                         "%dx-refined run gathered onto the coarse cells" % R},
+            "errors_vs_refined": ({"plain": dict(zip(names, err_p), cell_density_rel_l1=cd_p),
+                                   "learned": dict(zip(names, err_l), cell_density_rel_l1=cd_l),
+                                   "how": "mean over the mixed cells at t = 0.2 against the "
+                                          "%dx-refined run gathered onto the coarse cells" % R}
+                                  if "failed" not in rf else None),
             "against_plain": {"interface_shift_cells_max": shift,
                               "mixed_cell_density_l1_rel": l1_mixed,
                               "all_cell_density_l1_rel": l1_all},
@@ -804,8 +817,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--refine", type=int, default=0,
-                    help="closure workload: refinement of the sub-cell truth (0: 4, or 2 "
-                         "from 1200 cells across)")
+                    help="closure workload: refinement of the sub-cell truth (0: 4)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
