@@ -896,14 +896,17 @@ def main():
     fp = {"exact": abi.FP_EXACT, "fast": abi.FP_FAST, "mixed": abi.FP_MIXED}[args.fp]
 
     # ---------------- value: device-resident time loop ---------------------
-    # W warm-up steps (graph capture, caches), then the initial state is
-    # uploaded again and the timed run starts at t = 0: K steps, or with
+    # W warm-up steps, at least one whole graph of the device loop (16
+    # steps: its capture and instantiation, a host-side cost paid once per
+    # context, then falls outside the timed region), then the initial state
+    # is uploaded again and the timed run starts at t = 0: K steps, or with
     # K = 0 the whole run to time_end (the configuration's own end time).
     p = base.copy()
     s = Solver(p, fp_mode=fp)
     init = {fid: arr.copy() for fid, arr in p.fields.items()}
     ts0 = p.timestep.copy()
-    ierr, _ = s.run(max_steps=max(1, args.warmup), ts=p.timestep.copy(), history=False)
+    warm = max(16, args.warmup)
+    ierr, _ = s.run(max_steps=warm, ts=p.timestep.copy(), history=False)
     assert ierr == 0, s.error.message
     for fid, arr in init.items():
         np.copyto(p.fields[fid], arr)
@@ -1029,7 +1032,7 @@ def main():
     if rank == 0:
         line = {"metric": METRIC, "value": value,
                 "unit": "zone-cycles/s", "n_gpus": world, "steps": nsteps,
-                "warmup": args.warmup, "ms_per_step": t_max / max(1, nsteps),
+                "warmup": warm, "ms_per_step": t_max / max(1, nsteps),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64", "data": "synthetic",
                 "config": {"workload": wname, "nel": nel, "fp_mode": args.fp,
