@@ -15,7 +15,8 @@ runs the same steps in both floating-point modes:
 Configurations: Sod 400x40 to t = 0.2 (checkpoints every 50 steps),
 Sedov 512x512 with the benchmark's hourglass and sub-zonal settings for
 100 steps, Sedov 128x128 with them to t = 1, Noh 2048x2048 Lagrangian and
-Eulerian for 5 steps.
+Eulerian for 5 steps, and Noh Lagrangian on the reference's own polar mesh
+(150x60, the family of input/noh_small) to t = 0.6.
 """
 import numpy as np
 import pytest
@@ -131,6 +132,8 @@ BASELINE = {
     "sedov_128_bench_t1": (lambda: configs.sedov(128, kappa=0.01, pmerit=0.1), None, 0),
     "noh_2048_lagrangian_5steps": (lambda: configs.noh(2048), 5, 0),
     "noh_2048_eulerian_5steps": (lambda: configs.noh(2048, eulerian=True), 5, 0),
+    # the reference's own polar Noh mesh (input/noh_small's family), to t = 0.6
+    "noh_polar_150x60_t0.6": (lambda: configs.noh_polar(150, 60), None, 2000),
 }
 
 
