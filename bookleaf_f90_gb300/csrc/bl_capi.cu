@@ -19,6 +19,7 @@
 #include "bl_ctx.h"
 #include "bl_kernels.h"
 #include "bl_mma.cuh"
+#include "bl_setup.cuh"
 
 using bl::DevStep;
 using bl::d4;
@@ -80,17 +81,32 @@ bool reject_batch(bl_ctx* x, bl_error* e, const char* where) {
   return true;
 }
 
+// Device arrays come from a per-context arena: chunks of at least 64 MB
+// (doubling), each allocated and zeroed once, carved in 256-byte aligned
+// pieces, so that a context's few dozen arrays cost a handful of
+// cudaMalloc calls instead of one each.  Every piece starts zeroed.
 template <class T>
 T* dalloc(bl_ctx* x, size_t n, cudaError_t& st) {
   if (n == 0) n = 1;
-  void* p = nullptr;
-  cudaError_t r = cudaMalloc(&p, n * sizeof(T));
-  if (r != cudaSuccess) {
-    st = r;
-    return nullptr;
+  const size_t bytes = (n * sizeof(T) + 255) & ~(size_t)255;
+  if (x->arena_left < bytes) {
+    size_t sz = x->arena_next < ((size_t)64 << 20) ? ((size_t)64 << 20) : x->arena_next;
+    if (sz < bytes) sz = bytes;
+    void* p = nullptr;
+    cudaError_t r = cudaMalloc(&p, sz);
+    if (r != cudaSuccess) {
+      st = r;
+      return nullptr;
+    }
+    cudaMemsetAsync(p, 0, sz, x->stream);
+    x->bufs.push_back(p);
+    x->arena_ptr = static_cast<char*>(p);
+    x->arena_left = sz;
+    x->arena_next = 2 * sz;
   }
-  cudaMemsetAsync(p, 0, n * sizeof(T), x->stream);
-  x->bufs.push_back(p);
+  void* p = x->arena_ptr;
+  x->arena_ptr += bytes;
+  x->arena_left -= bytes;
   return static_cast<T*>(p);
 }
 
@@ -305,42 +321,23 @@ int init_impl(bl_ctx** out, const bl_sizes* sizes, const bl_config* config, void
   const int* ielfc = static_cast<const int*>(dh[BL_IELFC]);
   const int* ielreg = static_cast<const int*>(dh[BL_IELREG]);
   const int* srt1 = static_cast<const int*>(dh[BL_IELSORT1]);
-  // host-side bounds validation before anything reaches the device
-  for (long k = 0; k < 4L * nel; k++) {
-    if (ielnd[k] < 1 || ielnd[k] > nnd || ielel[k] < 1 || ielel[k] > nel || ielfc[k] < 1 ||
-        ielfc[k] > 4) {
-      set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init: connectivity out of range");
-      return BL_FAILURE;
-    }
-  }
-  for (int i = 0; i < nel; i++)
-    if (ielreg[i] < 1 || ielreg[i] > s.nreg || srt1[i] < 1 || srt1[i] > nel) {
-      set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init: ielreg/ielsort1 out of range");
-      return BL_FAILURE;
-    }
   const int* ielmat = static_cast<const int*>(dh[BL_IELMAT]);
-  for (int i = 0; i < nel; i++)
-    if (ielmat[i] > s.nmat) {
-      set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init: ielmat out of range");
-      return BL_FAILURE;
-    }
+  // Checks on the host, reported after the connectivity's (checked on the
+  // device below): ielsort2 and the mixed-cell lists.
+  const char* herr = nullptr;
   if (c.ale_zexist) {
     const int* srt2 = static_cast<const int*>(dh[BL_IELSORT2]);
     if (!srt2) {
-      set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init: ielsort2 needed for ALE");
-      return BL_FAILURE;
+      herr = "ERROR: bl_init: ielsort2 needed for ALE";
+    } else {
+      // serial BookLeaf sets ielsort2 to the identity (init_dr_utils.f90:65-68);
+      // ale_kn_updatend sums in natural order, calcbasisnd in ielsort2 order
+      for (int i = 0; i < nel && !herr; i++)
+        if (srt2[i] != i + 1) herr = "ERROR: bl_init: ielsort2 must be the identity for one partition";
     }
-    for (int i = 0; i < nel; i++)
-      if (srt2[i] != i + 1) {
-        // serial BookLeaf sets ielsort2 to the identity (init_dr_utils.f90:65-68);
-        // ale_kn_updatend sums in natural order, calcbasisnd in ielsort2 order
-        set_err(error, BL_FAILURE, BL_HALT_ALL,
-                "ERROR: bl_init: ielsort2 must be the identity for one partition");
-        return BL_FAILURE;
-      }
   }
   std::vector<int> elmx(nel, -1);
-  if (ncp > 0) {
+  if (ncp > 0 && !herr) {
     const int* imxel = static_cast<const int*>(dh[BL_IMXEL]);
     const int* imxfcp = static_cast<const int*>(dh[BL_IMXFCP]);
     const int* imxncp = static_cast<const int*>(dh[BL_IMXNCP]);
@@ -349,23 +346,16 @@ int init_impl(bl_ctx** out, const bl_sizes* sizes, const bl_config* config, void
                                  BL_FRVOLUME, BL_CPMASS, BL_FRMASS};
     bool ok = imxel && imxfcp && imxncp && icpmat;
     for (int id : cpneed) ok = ok && dh[id];
-    if (!ok) {
-      set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init: component fields missing");
-      return BL_FAILURE;
-    }
-    for (int m = 0; m < nmx; m++) {
+    if (!ok) herr = "ERROR: bl_init: component fields missing";
+    for (int m = 0; m < nmx && !herr; m++) {
       if (imxel[m] < 1 || imxel[m] > nel || imxfcp[m] < 1 || imxncp[m] < 1 ||
-          imxfcp[m] + imxncp[m] - 1 > ncp) {
-        set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init: mixed-cell lists out of range");
-        return BL_FAILURE;
-      }
-      elmx[imxel[m] - 1] = m;
+          imxfcp[m] + imxncp[m] - 1 > ncp)
+        herr = "ERROR: bl_init: mixed-cell lists out of range";
+      else
+        elmx[imxel[m] - 1] = m;
     }
-    for (int k = 0; k < ncp; k++)
-      if (icpmat[k] < 0 || icpmat[k] > s.nmat) {
-        set_err(error, BL_FAILURE, BL_HALT_ALL, "ERROR: bl_init: icpmat out of range");
-        return BL_FAILURE;
-      }
+    for (int k = 0; k < ncp && !herr; k++)
+      if (icpmat[k] < 0 || icpmat[k] > s.nmat) herr = "ERROR: bl_init: icpmat out of range";
   }
 
   bl_ctx* x = new bl_ctx();
@@ -387,73 +377,90 @@ int init_impl(bl_ctx** out, const bl_sizes* sizes, const bl_config* config, void
   F.nnd = nnd;
   F.ncp = ncp;
   F.nmx = nmx;
-  // ---- connectivity, converted to 0-based
+  // ---- connectivity: uploaded as the caller holds it, checked and
+  // converted to 0-based on the device (bl_setup.cuh); nothing indexes
+  // with it before the host has read the check's error bits
   {
-    std::vector<int4> nd(nel), ee(nel);
-    std::vector<int> fc(nel), rg(nel);
-    for (int i = 0; i < nel; i++) {
-      nd[i] = make_int4(ielnd[4 * i] - 1, ielnd[4 * i + 1] - 1, ielnd[4 * i + 2] - 1,
-                        ielnd[4 * i + 3] - 1);
-      ee[i] = make_int4(ielel[4 * i] - 1, ielel[4 * i + 1] - 1, ielel[4 * i + 2] - 1,
-                        ielel[4 * i + 3] - 1);
-      fc[i] = (ielfc[4 * i] - 1) | ((ielfc[4 * i + 1] - 1) << 8) |
-              ((ielfc[4 * i + 2] - 1) << 16) | ((ielfc[4 * i + 3] - 1) << 24);
-      rg[i] = ielreg[i] - 1;
-    }
+    namespace su = bl::setup;
     int4* d_nd = dalloc<int4>(x, nel, st);
     int4* d_ee = dalloc<int4>(x, nel, st);
     int* d_fc = dalloc<int>(x, nel, st);
     int* d_rg = dalloc<int>(x, nel, st);
     int* d_mt = dalloc<int>(x, nel, st);
     int* d_it = dalloc<int>(x, nnd, st);
+    int* d_off = dalloc<int>(x, nnd + 1, st);
+    int* d_ent = dalloc<int>(x, 4L * nel, st);
+    // set-up scratch (stays with the context's arena: 8 bytes an element
+    // and 4 a node): ielsort1, its permutation counts, the node cursors,
+    // the scan's tile sums, the error bits
+    const int nb = su::blocks_for(nnd, su::kScanTile);
+    int* d_srt = dalloc<int>(x, nel, st);
+    int* d_seen = dalloc<int>(x, nel, st);
+    int* d_cnt = dalloc<int>(x, nnd, st);
+    int* d_bsum = dalloc<int>(x, nb, st);
+    int* d_bad = dalloc<int>(x, 1, st);
     if (st != cudaSuccess) goto fail;
-    up(x, d_nd, nd.data(), nel);
-    up(x, d_ee, ee.data(), nel);
-    up(x, d_fc, fc.data(), nel);
-    up(x, d_rg, rg.data(), nel);
+    up(x, d_nd, ielnd, nel);  // four nodes an element, as one int4
+    up(x, d_ee, ielel, nel);
+    up(x, reinterpret_cast<int4*>(d_ent), ielfc, nel);  // the faces, until the fill
+    up(x, d_rg, ielreg, nel);
     up(x, d_mt, ielmat, nel);
     up(x, d_it, dh[BL_INDTYPE], nnd);
+    up(x, d_srt, srt1, nel);
+    const int ge = su::blocks_for(nel, su::kThreads), gn = su::blocks_for(nnd, su::kThreads);
+    su::k_check_pack<<<ge, su::kThreads, 0, x->stream>>>(
+        d_nd, d_ee, reinterpret_cast<const int4*>(d_ent), d_fc, d_rg, d_srt, d_mt, d_seen, nel,
+        nnd, s.nreg, s.nmat, d_bad);
+    int bad = 0;
+    cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, x->stream);
+    r = cudaStreamSynchronize(x->stream);
+    if (r == cudaSuccess) r = cudaGetLastError();
+    if (r != cudaSuccess) {
+      st = r;
+      goto fail;
+    }
+    if (bad || herr) {
+      bl_finalize(x);
+      set_err(error, BL_FAILURE, BL_HALT_ALL,
+              (bad & su::kBadConn)      ? "ERROR: bl_init: connectivity out of range"
+              : (bad & su::kBadRegSort) ? "ERROR: bl_init: ielreg/ielsort1 out of range"
+              : (bad & su::kBadPerm)    ? "ERROR: bl_init: ielsort1 is not a permutation"
+              : (bad & su::kBadMat)     ? "ERROR: bl_init: ielmat out of range"
+                                        : herr);
+      return BL_FAILURE;
+    }
     F.ielnd = d_nd;
     F.ielel = d_ee;
     F.ielfc = d_fc;
     F.ielreg = d_rg;
     F.ielmat = d_mt;
     F.indtype = d_it;
-    cudaStreamSynchronize(x->stream);
-    // node -> corner CSR in hydro_kn_scatteracceleration's order: corner jj
-    // outer, elements in ielsort1 order inner (hydro_kn_getacceleration.f90:53-72)
-    std::vector<int> off(nnd + 1, 0), ent(4L * nel);
-    for (long k = 0; k < 4L * nel; k++) off[ielnd[k]]++;
-    for (int i = 0; i < nnd; i++) off[i + 1] += off[i];
-    std::vector<int> pos(off.begin(), off.end() - 1);
-    for (int jj = 0; jj < 4; jj++)
-      for (int kk = 0; kk < nel; kk++) {
-        const int iel = srt1[kk] - 1;
-        const int ind = ielnd[4 * iel + jj] - 1;
-        ent[pos[ind]++] = 4 * iel + jj;
-      }
-    int* d_off = dalloc<int>(x, nnd + 1, st);
-    int* d_ent = dalloc<int>(x, 4L * nel, st);
-    if (st != cudaSuccess) goto fail;
-    up(x, d_off, off.data(), nnd + 1);
-    up(x, d_ent, ent.data(), 4L * nel);
+    // node -> corner tables: counts and offsets (shared by both tables)
+    su::k_count<<<ge, su::kThreads, 0, x->stream>>>(d_nd, nel, nnd, d_cnt);
+    su::k_scan_tiles<<<nb, su::kThreads, 0, x->stream>>>(d_cnt, nnd, d_bsum);
+    su::k_scan_sums<<<1, su::kThreads, 0, x->stream>>>(d_bsum, nb);
+    su::k_scan_apply<<<nb, su::kThreads, 0, x->stream>>>(d_cnt, nnd, d_bsum, d_off);
+    // corner-major, hydro_kn_scatteracceleration's order: corner jj outer,
+    // elements in ielsort1 order inner (hydro_kn_getacceleration.f90:53-72)
+    su::k_fill<<<ge, su::kThreads, 0, x->stream>>>(d_nd, d_srt, nel, nnd, d_cnt, d_ent);
+    su::k_sort<<<gn, su::kThreads, 0, x->stream>>>(d_off, d_srt, nel, nnd, d_ent);
     F.nc_off = d_off;
     F.nc_ent = d_ent;
-    // element-major CSR (ale_kn_calcbasisnd / massbasisnd / updatend)
+    // element-major, natural order (ale_kn_calcbasisnd / massbasisnd / updatend)
     if (c.ale_zexist) {
-      std::vector<int> pos2(off.begin(), off.end() - 1), ent2(4L * nel);
-      for (int iel = 0; iel < nel; iel++)
-        for (int j = 0; j < 4; j++) {
-          const int ind = ielnd[4 * iel + j] - 1;
-          ent2[pos2[ind]++] = 4 * iel + j;
-        }
       int* d_ent2 = dalloc<int>(x, 4L * nel, st);
       if (st != cudaSuccess) goto fail;
-      up(x, d_ent2, ent2.data(), 4L * nel);
+      su::k_copy<<<gn, su::kThreads, 0, x->stream>>>(d_off, nnd, d_cnt);
+      su::k_fill<<<ge, su::kThreads, 0, x->stream>>>(d_nd, nullptr, nel, nnd, d_cnt, d_ent2);
+      su::k_sort<<<gn, su::kThreads, 0, x->stream>>>(d_off, nullptr, nel, nnd, d_ent2);
       F.ne_off = d_off;
       F.ne_ent = d_ent2;
     }
-    cudaStreamSynchronize(x->stream);
+    r = cudaGetLastError();
+    if (r != cudaSuccess) {
+      st = r;
+      goto fail;
+    }
   }
   // ---- node fields
   F.ndx = dalloc<double>(x, nnd, st);

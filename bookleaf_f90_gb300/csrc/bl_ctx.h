@@ -21,6 +21,9 @@ struct bl_ctx {
   bl::DevCfg C{};
   bl::Launchers L{};
   std::vector<void*> bufs;
+  // the device arena the arrays are carved from (dalloc)
+  char* arena_ptr = nullptr;
+  size_t arena_left = 0, arena_next = 0;
   bl::DevStep* hstep = nullptr;  // pinned mirror of F.step
   // true while *hstep equals F.step on the device: set by a completed
   // fetch of the header, cleared whenever work that may change it is queued
