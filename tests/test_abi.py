@@ -57,7 +57,8 @@ def test_init_fails_loudly_without_gpu(lib):
 
 
 def test_init_rejects_bad_connectivity(lib):
-    """Host-side bounds validation runs before anything reaches a device."""
+    """A bad node number is refused (on a machine without a GPU the refusal
+    is the missing device; the device-side check has its own tests)."""
     p = Problem.from_deck(configs.sod(8, 2))
     p.fields[abi.IELND][3, 1] = p.nnd + 5
     err = abi.Error()
