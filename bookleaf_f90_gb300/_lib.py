@@ -104,11 +104,10 @@ EXPORTS = ("bl_init", "bl_finalize", "bl_getdt", "bl_lagstep", "bl_alestep", "bl
 
 def fp64_rates():
     """Measured issue rates on the current device, G operations/s: FP64
-    FMA, hardware and integer-pipe divide, hardware and integer-pipe square
-    root."""
+    FMA, hardware and integer-pipe divide, square root and multiply."""
     L = load()
-    out = (ct.c_double * 5)()
-    if L.bl_fp64_rates(out, 5) != 0:
+    out = (ct.c_double * 7)()
+    if L.bl_fp64_rates(out, 7) != 0:
         raise RuntimeError("bl_fp64_rates failed")
     return {"dfma": out[0], "ddiv_hw": out[1], "ddiv_int": out[2], "dsqrt_hw": out[3],
-            "dsqrt_int": out[4]}
+            "dsqrt_int": out[4], "dmul_hw": out[5], "dmul_int": out[6]}

@@ -7,7 +7,9 @@
 // significands, ratios next to 1, exponent-range edges, zeros, infinities,
 // NaNs, subnormals of every width) and counts results that differ from the hardware in any
 // bit (two NaNs compare equal).  op 0 is the divide, op 1 the square root
-// (its operand is the first of the pair; for op 1 the second reports 0).
+// (its operand is the first of the pair; for op 1 the second reports 0),
+// op 2 the multiply (one pair in four with significands of 28 and 27 bits,
+// whose 54- and 55-bit products round from exact ties).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -68,6 +70,13 @@ __global__ void k_selftest(int op, long long n, unsigned long long seed,
       if ((r4 >> 60) == 0) a = b * __longlong_as_double((long long)(0x3FF0000000000000ull | (r1 & 0xF)));
       h = a / b;
       s = bl::ddiv_rn(a, b);
+    } else if (op == 2) {
+      if (((r4 >> 58) & 3) == 0) {
+        a = __longlong_as_double(__double_as_longlong(a) & ~((1ll << 25) - 1));
+        b = __longlong_as_double(__double_as_longlong(b) & ~((1ll << 26) - 1));
+      }
+      h = a * b;
+      s = bl::dmul_rn(a, b);
     } else {
       // squares of doubles and their neighbours, and integers next to squares
       const int kind = (int)((r4 >> 56) & 7);
@@ -96,7 +105,7 @@ __global__ void k_selftest(int op, long long n, unsigned long long seed,
 
 extern "C" int bl_selftest_fp64(int op, long long n, unsigned long long seed,
                                 long long* mismatches, double* first_a, double* first_b) {
-  if ((op != 0 && op != 1) || n < 0 || !mismatches) return BL_FAILURE;
+  if (op < 0 || op > 2 || n < 0 || !mismatches) return BL_FAILURE;
   unsigned long long* d = nullptr;
   if (cudaMalloc(&d, 3 * sizeof(unsigned long long)) != cudaSuccess) return BL_FAILURE;
   cudaMemset(d, 0, 3 * sizeof(unsigned long long));
@@ -149,6 +158,11 @@ __global__ void k_rate_op(double* out, int iters, double a) {
       x0 = bl::dsqrt_rn(x0) + 1.0; x1 = bl::dsqrt_rn(x1) + 1.0;
       x2 = bl::dsqrt_rn(x2) + 1.0; x3 = bl::dsqrt_rn(x3) + 1.0;
     }
+    if (OP == 4) { x0 = x0 * a; x1 = x1 * a; x2 = x2 * a; x3 = x3 * a; }
+    if (OP == 5) {
+      x0 = bl::dmul_rn(x0, a); x1 = bl::dmul_rn(x1, a);
+      x2 = bl::dmul_rn(x2, a); x3 = bl::dmul_rn(x3, a);
+    }
   }
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3;
 }
@@ -165,7 +179,8 @@ extern "C" int bl_fp64_rates(double* rates, int n) {
   cudaEventCreate(&e1);
   float ms = 0.f;
   int rc = BL_SUCCESS;
-  for (int which = 0; which < 5 && rc == BL_SUCCESS; which++) {
+  const int nrates = n >= 7 ? 7 : 5;
+  for (int which = 0; which < nrates && rc == BL_SUCCESS; which++) {
     const int iters = which == 0 ? 1024 : 128;
     const double ops = (which == 0 ? 8.0 : 4.0) * iters * (double)total;
     for (int rep = 0; rep < 2; rep++) {  // first pass warms up
@@ -175,7 +190,9 @@ extern "C" int bl_fp64_rates(double* rates, int n) {
         case 1: k_rate_op<0><<<kRateBlocks, kRateThreads>>>(d, iters, 3.0); break;
         case 2: k_rate_op<1><<<kRateBlocks, kRateThreads>>>(d, iters, 3.0); break;
         case 3: k_rate_op<2><<<kRateBlocks, kRateThreads>>>(d, iters, 0.0); break;
-        default: k_rate_op<3><<<kRateBlocks, kRateThreads>>>(d, iters, 0.0); break;
+        case 4: k_rate_op<3><<<kRateBlocks, kRateThreads>>>(d, iters, 0.0); break;
+        case 5: k_rate_op<4><<<kRateBlocks, kRateThreads>>>(d, iters, 0.9999999); break;
+        default: k_rate_op<5><<<kRateBlocks, kRateThreads>>>(d, iters, 0.9999999); break;
       }
       cudaEventRecord(e1);
       if (cudaEventSynchronize(e1) != cudaSuccess) { rc = BL_FAILURE; break; }

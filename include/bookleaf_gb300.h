@@ -326,13 +326,15 @@ const char *bl_version(void);
  * operands (random, plus hard cases) are computed both ways on the current
  * device; *mismatches receives the number of results that differ in any
  * bit, first_a/first_b the first failing operands.  op 0: division a/b;
- * op 1: square root of a.  Returns 0, or -1 when CUDA fails. */
+ * op 1: square root of a; op 2: product a*b.  Returns 0, or -1 when CUDA
+ * fails. */
 int bl_selftest_fp64(int op, long long n, unsigned long long seed, long long *mismatches,
                      double *first_a, double *first_b);
 
 /* Issue rates on the current device, in G operations/s (no counterpart in
  * the reference): rates[0] FP64 FMA, [1] hardware divide, [2] integer-pipe
- * divide, [3] hardware square root, [4] integer-pipe square root.  n >= 5.
+ * divide, [3] hardware square root, [4] integer-pipe square root, and when
+ * n >= 7 [5] hardware multiply, [6] integer-pipe multiply.  n >= 5.
  * The FMA rate is the FP64 roof the hot path's kernels are measured
  * against.  Returns 0, or -1 when CUDA fails. */
 int bl_fp64_rates(double *rates, int n);

@@ -1,5 +1,6 @@
-"""The integer-pipe FP64 divide and square root the kernels use must equal
-the hardware operations bit for bit (bl_fp64.cuh, checked on the device)."""
+"""The integer-pipe FP64 divide, square root and multiply the kernels use
+must equal the hardware operations bit for bit (bl_fp64.cuh, checked on the
+device)."""
 import ctypes as ct
 
 import pytest
@@ -27,6 +28,12 @@ def test_divide_matches_hardware(seed):
 def test_sqrt_matches_hardware(seed):
     bad, a, _ = _selftest(1, 1 << 28, seed)
     assert bad == 0, "first mismatch sqrt(%r)" % (a,)
+
+
+@pytest.mark.parametrize("seed", [3, 0xD1CE, 0x7E57AB1E])
+def test_multiply_matches_hardware(seed):
+    bad, a, b = _selftest(2, 1 << 28, seed)
+    assert bad == 0, "first mismatch %r * %r" % (a, b)
 
 
 def test_integer_pipe_rates_beat_hardware():
