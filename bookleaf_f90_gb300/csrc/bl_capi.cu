@@ -967,6 +967,16 @@ int bl_time_step_kernels(bl_ctx* x, bl_timestep* ts, int nstep, double* ms, int 
   return BL_SUCCESS;
 }
 
+// corner coordinates: out[e] = the element's four node values (the host's
+// (4, nel) corner layout)
+__global__ void k_cngather(const int4* __restrict__ ielnd, const double* __restrict__ nd,
+                           int nel, d4* __restrict__ out) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nel) return;
+  const int4 n = ielnd[e];
+  out[e] = bl::make_d4(nd[n.x], nd[n.y], nd[n.z], nd[n.w]);
+}
+
 static size_t field_count(const bl_ctx* x, int id, int& kind) {
   // kind: 0 double element, 1 double corner, 2 double node, 3 double comp,
   //       4 derived (cnx/cny/cpa*), -1 not a device state field
@@ -1035,46 +1045,68 @@ static void* dev_ptr(bl_ctx* x, int id) {
 
 int bl_sync_to_host(bl_ctx* x, int id) {
   if (!x) return BL_FAILURE;
-  if (id == 0) {
-    for (int k : kStateIds) {
-      int rc = bl_sync_to_host(x, k);
-      if (rc != BL_SUCCESS) return rc;
-    }
-    return BL_SUCCESS;
-  }
-  if (id < 1 || id > BL_NID || !x->host[id]) return BL_SUCCESS;
-  int kind;
-  size_t n = field_count(x, id, kind);
-  if (kind < 0) return BL_SUCCESS;
-  cudaError_t r;
-  if (kind == 4) {
-    // derived fields: cnx/cny = node positions gathered to corners
-    // (utils_kn_cngather); cpa*/cpb* = element terms gathered to components
-    const int* ielnd = static_cast<const int*>(x->host[BL_IELND]);
-    double* h = static_cast<double*>(x->host[id]);
-    if (id == BL_CNX || id == BL_CNY) {
-      std::vector<double> nd(x->s.nnd);
-      r = cudaMemcpy(nd.data(), id == BL_CNX ? x->F.ndx : x->F.ndy, sizeof(double) * x->s.nnd,
-                     cudaMemcpyDeviceToHost);
-      if (r != cudaSuccess) return BL_FAILURE;
-      for (size_t k = 0; k < n; k++) h[k] = nd[ielnd[k] - 1];
+  if (id != 0 && (id < 1 || id > BL_NID)) return BL_SUCCESS;
+  const int* ids = id == 0 ? kStateIds : &id;
+  const int nids = id == 0 ? (int)(sizeof kStateIds / sizeof kStateIds[0]) : 1;
+  // every copy queued on the context's stream, one wait for all of them;
+  // the corner coordinates (utils_kn_cngather of the node positions) are
+  // gathered on the device first
+  bool gathered_cp = false;
+  for (int k = 0; k < nids; k++) {
+    const int f = ids[k];
+    if (!x->host[f]) continue;
+    int kind;
+    const size_t n = field_count(x, f, kind);
+    if (kind < 0) continue;
+    if (kind == 4) {
+      if (f != BL_CNX && f != BL_CNY) {
+        gathered_cp = true;  // component terms: after the wait
+        continue;
+      }
+      if (!x->cn_gather) {
+        cudaError_t st = cudaSuccess;
+        x->cn_gather = dalloc<double>(x, 8L * x->s.nel, st);
+        if (st != cudaSuccess) return BL_FAILURE;
+      }
+      double* g = x->cn_gather + (f == BL_CNY ? 4L * x->s.nel : 0);
+      k_cngather<<<(x->s.nel + 255) / 256, 256, 0, x->stream>>>(
+          x->F.ielnd, f == BL_CNX ? x->F.ndx : x->F.ndy, x->s.nel, reinterpret_cast<d4*>(g));
+      cudaMemcpyAsync(x->host[f], g, n * sizeof(double), cudaMemcpyDeviceToHost, x->stream);
     } else {
-      const double* src = id == BL_CPA1 ? x->F.a1 : id == BL_CPA3 ? x->F.a3 : id == BL_CPB1 ? x->F.b1 : x->F.b3;
-      std::vector<double> el(x->s.nel);
+      cudaMemcpyAsync(x->host[f], dev_ptr(x, f), n * sizeof(double), cudaMemcpyDeviceToHost,
+                      x->stream);
+    }
+  }
+  cudaError_t r = cudaStreamSynchronize(x->stream);
+  if (r == cudaSuccess) r = cudaGetLastError();
+  if (r != cudaSuccess) return BL_FAILURE;
+  // component iso terms: the element terms gathered to components
+  if (gathered_cp) {
+    std::vector<double> el(x->s.nel);
+    const int* imxel = static_cast<const int*>(x->host[BL_IMXEL]);
+    const int* imxfcp = static_cast<const int*>(x->host[BL_IMXFCP]);
+    const int* imxncp = static_cast<const int*>(x->host[BL_IMXNCP]);
+    for (int k = 0; k < nids; k++) {
+      const int f = ids[k];
+      if (!x->host[f] || (f != BL_CPA1 && f != BL_CPA3 && f != BL_CPB1 && f != BL_CPB3)) continue;
+      int kind;
+      field_count(x, f, kind);
+      if (kind != 4) continue;
+      const double* src = f == BL_CPA1 ? x->F.a1 : f == BL_CPA3 ? x->F.a3 : f == BL_CPB1 ? x->F.b1 : x->F.b3;
       r = cudaMemcpy(el.data(), src, sizeof(double) * x->s.nel, cudaMemcpyDeviceToHost);
       if (r != cudaSuccess) return BL_FAILURE;
-      const int* imxel = static_cast<const int*>(x->host[BL_IMXEL]);
-      const int* imxfcp = static_cast<const int*>(x->host[BL_IMXFCP]);
-      const int* imxncp = static_cast<const int*>(x->host[BL_IMXNCP]);
+      double* h = static_cast<double*>(x->host[f]);
       for (int m = 0; m < x->s.nmx; m++)
-        for (int k = 0; k < imxncp[m]; k++) h[imxfcp[m] - 1 + k] = el[imxel[m] - 1];
+        for (int c = 0; c < imxncp[m]; c++) h[imxfcp[m] - 1 + c] = el[imxel[m] - 1];
     }
-    if (x->ninst > 0) batch_copy(x, id, true);
-    return BL_SUCCESS;
   }
-  r = cudaMemcpy(x->host[id], dev_ptr(x, id), n * sizeof(double), cudaMemcpyDeviceToHost);
-  if (r == cudaSuccess && x->ninst > 0) batch_copy(x, id, true);
-  return r == cudaSuccess ? BL_SUCCESS : BL_FAILURE;
+  if (x->ninst > 0)
+    for (int k = 0; k < nids; k++) {
+      int kind;
+      field_count(x, ids[k], kind);
+      if (kind >= 0 && x->host[ids[k]]) batch_copy(x, ids[k], true);
+    }
+  return BL_SUCCESS;
 }
 
 int bl_sync_to_device(bl_ctx* x, int id) {

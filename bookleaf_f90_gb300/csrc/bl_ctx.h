@@ -24,6 +24,7 @@ struct bl_ctx {
   // the device arena the arrays are carved from (dalloc)
   char* arena_ptr = nullptr;
   size_t arena_left = 0, arena_next = 0;
+  double* cn_gather = nullptr;  // [2][4*nel]: cnx, cny gathered for bl_sync_to_host
   bl::DevStep* hstep = nullptr;  // pinned mirror of F.step
   // true while *hstep equals F.step on the device: set by a completed
   // fetch of the header, cleared whenever work that may change it is queued

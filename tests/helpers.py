@@ -7,7 +7,8 @@ from bookleaf_f90_gb300 import Problem, Solver, abi, configs  # noqa: F401
 STATE = [abi.ELDENSITY, abi.ELENERGY, abi.ELPRESSURE, abi.ELCS2, abi.ELVOLUME, abi.A1,
          abi.A2, abi.A3, abi.B1, abi.B2, abi.B3, abi.CNWT, abi.CNX, abi.CNY, abi.CNVISCX,
          abi.CNVISCY, abi.ELVISC, abi.ELMASS, abi.CNMASS, abi.NDX, abi.NDY, abi.NDU, abi.NDV]
-CPSTATE = [abi.CPDENSITY, abi.CPENERGY, abi.CPPRESSURE, abi.CPCS2, abi.CPVOLUME]
+CPSTATE = [abi.CPDENSITY, abi.CPENERGY, abi.CPPRESSURE, abi.CPCS2, abi.CPVOLUME,
+           abi.CPA1, abi.CPA3, abi.CPB1, abi.CPB3]
 
 
 def state_ids(p):
