@@ -157,8 +157,14 @@ enum { BL_DT_MAXIMUM = 0, BL_DT_GROWTH = 1, BL_DT_INITIAL = 2, BL_DT_CFL = 3,
  * and (if zsp) spmass.  dh has BL_NID+1 entries; dh[0] is unused and dh[id]
  * is the host array of field id (NULL for fields the path does not need:
  * scratch, component arrays when ncp==0, spmass when zsp is false,
- * ielsort2 when there is no ALE).  fp_mode is BL_FP_FAST or BL_FP_EXACT.
- * The device ordinal is the current CUDA device of the calling thread. */
+ * ielsort2 when there is no ALE).  fp_mode is BL_FP_FAST, BL_FP_EXACT or
+ * BL_FP_MIXED.  The device ordinal is the current CUDA device of the
+ * calling thread.  The connectivity is checked on the device before any
+ * kernel indexes with it; a bad table returns BL_FAILURE with HALT_ALL and,
+ * in this order of precedence, "connectivity out of range" (ielnd, ielel,
+ * ielfc), "ielreg/ielsort1 out of range", "ielsort1 is not a permutation",
+ * "ielmat out of range", then the host's checks of ielsort2 and the
+ * mixed-cell lists. */
 int bl_init(bl_ctx **ctx, const bl_sizes *sizes, const bl_config *config,
             void *const *dh, int fp_mode, bl_error *error);
 
