@@ -15,8 +15,9 @@ runs the same steps in both floating-point modes:
 Configurations: Sod 400x40 to t = 0.2 (checkpoints every 50 steps),
 Sedov 512x512 with the benchmark's hourglass and sub-zonal settings for
 100 steps, Sedov 128x128 with them to t = 1, Noh 2048x2048 Lagrangian and
-Eulerian for 5 steps, and Noh Lagrangian on the reference's own polar mesh
-(150x60, the family of input/noh_small) to t = 0.6.
+Eulerian for 5 steps, Noh Lagrangian on the reference's own polar mesh
+(150x60, the family of input/noh_small) to t = 0.6, and the two-material
+Sod at 2000x200 with its mixed cells for 200 steps.
 """
 import numpy as np
 import pytest
@@ -64,7 +65,7 @@ _CACHE = {}
 def _oracle(name, deck, nsteps, every):
     if name not in _CACHE:
         _CACHE.clear()   # keep one case's checkpoints in host memory at a time
-        base = Problem.from_deck(deck)
+        base = deck if isinstance(deck, Problem) else Problem.from_deck(deck)
         _CACHE[name] = (base, _oracle_run(base, nsteps, every))
     return _CACHE[name]
 
@@ -134,7 +135,18 @@ BASELINE = {
     "noh_2048_eulerian_5steps": (lambda: configs.noh(2048, eulerian=True), 5, 0),
     # the reference's own polar Noh mesh (input/noh_small's family), to t = 0.6
     "noh_polar_150x60_t0.6": (lambda: configs.noh_polar(150, 60), None, 2000),
+    # the two-material Sod at its stated size with mixed cells: the planar
+    # interface tilted by 0.2 (right state rho = p = 0.5) the closure
+    # benchmark measures, cells cut by it made mixed with their exact area
+    # fractions; 200 steps
+    "sod2mat_2000x200_tilted_200steps": (lambda: _sod2mat(2000, 200), 200, 100),
 }
+
+
+def _sod2mat(nx, ny):
+    deck, frac = configs.sod_interface(nx, ny, time_end=0.2, amplitude=0.0, periods=0,
+                                       tilt=0.2, rho_right=0.5, p_right=0.5)
+    return Problem.from_deck(deck, material_fraction=frac)
 
 
 @pytest.mark.parametrize("mode", [abi.FP_EXACT, abi.FP_FAST], ids=["exact", "fast"])
