@@ -216,10 +216,15 @@ __global__ void k_mlp_image(const float* P, float* img) {
 
 // Adam on the FP32 master parameters (Kingma and Ba, 2015).
 // The image is kept current with the parameters.
+// Adam; the bias corrections of this update are entry *ebase + k of the
+// tables c1t, c2t (the mini-batch k of an epoch whose first update is
+// *ebase), so that one captured epoch replays with the next epoch's values
 __global__ void k_mlp_adam(float* P, float* M, float* V, float* img, const float* grad, float lr,
-                           float b1, float b2, float eps, float c1, float c2) {
+                           float b1, float b2, float eps, const float* c1t, const float* c2t,
+                           const int* ebase, int k) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= NP) return;
+  const float c1 = c1t[*ebase + k], c2 = c2t[*ebase + k];
   const float g = grad[i];
   const float m = b1 * M[i] + (1.0f - b1) * g, v = b2 * V[i] + (1.0f - b2) * g * g;
   M[i] = m;
@@ -340,19 +345,56 @@ int bl_mlp_train(bl_mlp* m, const float* x, const float* t, int n, int epochs, i
                  float lr, unsigned long long seed, float* losses) {
   if (!m || !x || !t || n < 1 || epochs < 1 || batch < SPB) return BL_FAILURE;
   const int nb_per = (batch + SPB - 1) / SPB;
-  float *dx = nullptr, *dt = nullptr, *G = nullptr, *L = nullptr;
-  int* didx = nullptr;
+  const int nbat = (n + batch - 1) / batch;  // mini-batches per epoch
+  const long nupd = (long)epochs * nbat;
+  float *dx = nullptr, *dt = nullptr, *G = nullptr, *L = nullptr, *c1t = nullptr, *c2t = nullptr;
+  int *didx = nullptr, *ebase = nullptr;
   bool ok = cudaMalloc(&dx, (size_t)n * NI * sizeof(float)) == cudaSuccess &&
             cudaMalloc(&dt, (size_t)n * NO * sizeof(float)) == cudaSuccess &&
             cudaMalloc(&didx, (size_t)n * sizeof(int)) == cudaSuccess &&
             cudaMalloc(&G, (size_t)nb_per * NP * sizeof(float)) == cudaSuccess &&
-            cudaMalloc(&L, (size_t)nb_per * sizeof(float)) == cudaSuccess;
+            cudaMalloc(&L, (size_t)nb_per * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&c1t, (size_t)nupd * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&c2t, (size_t)nupd * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&ebase, sizeof(int)) == cudaSuccess;
   ok = ok && cudaMemcpy(dx, x, (size_t)n * NI * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess &&
        cudaMemcpy(dt, t, (size_t)n * NO * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  // Adam's bias corrections for every update of the run (update u has step
+  // count m->step + 1 + u)
+  if (ok) {
+    std::vector<float> c1(nupd), c2(nupd);
+    for (long u = 0; u < nupd; u++) {
+      const float st = (float)(m->step + 1 + u);
+      c1[u] = 1.0f / (1.0f - powf(b1, st));
+      c2[u] = 1.0f / (1.0f - powf(b2, st));
+    }
+    ok = cudaMemcpy(c1t, c1.data(), nupd * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(c2t, c2.data(), nupd * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
+  }
+  // one epoch's mini-batches (gradient, block sum, Adam for each) captured
+  // once as a graph and replayed every epoch: the launches of a 256-sample
+  // mini-batch take longer to issue than to run
+  cudaStream_t cs = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  ok = ok && cudaStreamCreate(&cs) == cudaSuccess &&
+       cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+  if (ok) {
+    for (int k = 0; k < nbat; k++) {
+      const int b0 = k * batch, nb = std::min(batch, n - b0);
+      const int nblk = (nb + SPB - 1) / SPB;
+      k_mlp_grad<<<nblk, TPB, kSmemGrad, cs>>>(m->img, dx, dt, didx + b0, nb, 1.0f / (float)nb, G, L);
+      k_mlp_reduce<<<(NP + 255) / 256, 256, 0, cs>>>(G, L, nblk, m->grad, m->loss, m->acc, (double)nb);
+      k_mlp_adam<<<(NP + 255) / 256, 256, 0, cs>>>(m->P, m->M, m->V, m->img, m->grad, lr, b1, b2,
+                                                   eps, c1t, c2t, ebase, k);
+    }
+    ok = cudaStreamEndCapture(cs, &graph) == cudaSuccess &&
+         cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+  }
   std::vector<int> perm(n);
   for (int i = 0; i < n; i++) perm[i] = i;
   uint64_t r = seed * 0x9E3779B97F4A7C15ull + 1;
-  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
   for (int ep = 0; ep < epochs && ok; ep++) {
     // Fisher-Yates shuffle with a splitmix-style generator
     for (int i = n - 1; i > 0; i--) {
@@ -364,32 +406,29 @@ int bl_mlp_train(bl_mlp* m, const float* x, const float* t, int n, int epochs, i
       const int j = (int)(z % (uint64_t)(i + 1));
       std::swap(perm[i], perm[j]);
     }
-    ok = cudaMemcpy(didx, perm.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess &&
-         cudaMemset(m->acc, 0, sizeof(double)) == cudaSuccess;
-    // the epoch's mini-batches queue without host round trips; its loss is
-    // summed on the device and read once
-    for (int b0 = 0; b0 < n && ok; b0 += batch) {
-      const int nb = std::min(batch, n - b0);
-      const int nblk = (nb + SPB - 1) / SPB;
-      k_mlp_grad<<<nblk, TPB, kSmemGrad>>>(m->img, dx, dt, didx + b0, nb, 1.0f / (float)nb, G, L);
-      k_mlp_reduce<<<(NP + 255) / 256, 256>>>(G, L, nblk, m->grad, m->loss, m->acc, (double)nb);
-      m->step++;
-      const float c1 = 1.0f / (1.0f - powf(b1, (float)m->step));
-      const float c2 = 1.0f / (1.0f - powf(b2, (float)m->step));
-      k_mlp_adam<<<(NP + 255) / 256, 256>>>(m->P, m->M, m->V, m->img, m->grad, lr, b1, b2, eps,
-                                            c1, c2);
-    }
+    const int eb = ep * nbat;
     double eloss = 0.0;
-    ok = ok && cudaGetLastError() == cudaSuccess &&
-         cudaMemcpy(&eloss, m->acc, sizeof(double), cudaMemcpyDeviceToHost) == cudaSuccess;
+    ok = cudaMemcpyAsync(didx, perm.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, cs) == cudaSuccess &&
+         cudaMemcpyAsync(ebase, &eb, sizeof(int), cudaMemcpyHostToDevice, cs) == cudaSuccess &&
+         cudaMemsetAsync(m->acc, 0, sizeof(double), cs) == cudaSuccess &&
+         cudaGraphLaunch(exec, cs) == cudaSuccess &&
+         cudaMemcpyAsync(&eloss, m->acc, sizeof(double), cudaMemcpyDeviceToHost, cs) == cudaSuccess &&
+         cudaStreamSynchronize(cs) == cudaSuccess;
     if (losses) losses[ep] = (float)(eloss / n);
   }
-  ok = ok && cudaDeviceSynchronize() == cudaSuccess;
+  if (ok) m->step += (int)nupd;
+  ok = ok && cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess;
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  if (cs) cudaStreamDestroy(cs);
   cudaFree(dx);
   cudaFree(dt);
   cudaFree(didx);
   cudaFree(G);
   cudaFree(L);
+  cudaFree(c1t);
+  cudaFree(c2t);
+  cudaFree(ebase);
   return ok ? BL_SUCCESS : BL_FAILURE;
 }
 
