@@ -34,9 +34,11 @@
 #include "bl_kernels.h"
 #include "bl_mma.cuh"
 
-// Every FP64 division and square root of the path goes through the
-// integer-pipe versions, which return the IEEE results bit for bit
-// (bl_fp64.cuh).
+// Every FP64 division and square root of the per-element work goes
+// through the integer-pipe versions, which return the IEEE results bit for
+// bit (bl_fp64.cuh); the three of the dt reduction's last block, one
+// thread on the kernel's serial tail, use the hardware's (the same bits at
+// a fraction of the latency).
 // The divides and square roots run out of line: one body per kernel instead
 // of ~60 inlined copies of ~100 instructions, which overflowed the
 // instruction cache (k_getdt stalled on instruction fetch); measured on the
@@ -683,6 +685,8 @@ __device__ __forceinline__ void getdt_finish(const DevFields& F, const DevCfg& C
   // Each thread takes the partials b = tid, tid + BS, ... in that order as
   // before, eight at a time: their loads (L2, past the L1 that may not see
   // other blocks' writes) are all in flight before the first comparison.
+  // (Sixteen at a time, one round fewer on a 512x512 mesh, spilled in the
+  // rest of the kernel and made it slower.)
   {
     constexpr int U = 8;
     const double2* rv = reinterpret_cast<const double2*>(F.red_v) + blk0;
@@ -739,8 +743,11 @@ __device__ __forceinline__ void getdt_finish(const DevFields& F, const DevCfg& C
     if (S->run_mode) S->halted = 1;
     return;
   }
-  const double rdt_cfl = C.cfl_sf * SQRT(cflv);
-  const double rdt_div = DIV(C.div_sf, divv);
+  // one thread's three operations: the hardware's correctly rounded
+  // square root and divide (the same results as the integer-pipe routines,
+  // at a fraction of their latency on the serial tail)
+  const double rdt_cfl = C.cfl_sf * sqrt(cflv);
+  const double rdt_div = C.div_sf / divv;
   // 1-based element numbers local to the mesh (0: none)
   const int cfln = cfli >= 0 && cfli != 0x7fffffff ? cfli - el0 + 1 : 0;
   const int divn = divi >= 0 ? divi - el0 + 1 : 0;
@@ -760,7 +767,7 @@ __device__ __forceinline__ void getdt_finish(const DevFields& F, const DevCfg& C
   if (rdt_div < mind) { mind = rdt_div; mini = divn; mins = 4; }
   S->nstep = S->nstep + 1;
   S->dt = mind;
-  S->rdt = DIV(1.0, mind);
+  S->rdt = 1.0 / mind;
   S->sdt = mins;
   S->idtel = mini;
   S->time = S->time + mind;
