@@ -256,7 +256,7 @@ def cpu_baseline(deck, nel, target_s=12.0, cores=1, steps=0, warmup=1):
     return rate, steps, max(t for _, t in res)
 
 
-def run_ensemble(args, torch):
+def run_ensemble(args, torch, rank=0, world=1):
     """The batched ensemble (--workload ensemble; --size = number of meshes,
     default 512): every mesh of configs.ensemble advanced together by
     bl_run_batch, in the floating-point mode --fp selects (mixed: the
@@ -268,7 +268,13 @@ def run_ensemble(args, torch):
     and is set up again from the meshes still running whenever they hold
     less than half its elements (BatchSolver.run_compacting).  The batch's
     L1 errors against the FP64 per-mesh results are reported per mesh at
-    the end time and after 50 steps of both (the same step count)."""
+    the end time and after 50 steps of both (the same step count).  Under
+    torchrun each rank takes its share of the meshes (replicas.shard: by
+    elements times resolution, the step count growing with it) and runs
+    them as one GPU does; the rates are the zone-cycles of all ranks over
+    the slowest rank's time, and rank 0 gathers the per-mesh errors (the
+    ensemble is fixed: strong scaling).  Returns the line on rank 0, None
+    on the others."""
     from bookleaf_f90_gb300 import BatchSolver, Problem, Solver, abi, configs
     import ctypes as ct
     n = args.size or 512
@@ -277,7 +283,19 @@ def run_ensemble(args, torch):
     W = max(1, args.warmup)
     fp = {"exact": abi.FP_EXACT, "fast": abi.FP_FAST, "mixed": abi.FP_MIXED}[args.fp]
     fp_plain = abi.FP_EXACT if args.fp == "exact" else abi.FP_FAST
+    from bookleaf_f90_gb300.replicas import gather_to_root, job_rate, shard
     items = configs.ensemble(n, seed=seed)
+    weights = [m["nx"] * m["ny"] * max(m["nx"], m["ny"]) for _, m in items]
+    mine = shard(weights, world, rank)
+    items = [items[i] for i in mine]
+    dev = "cuda" if world > 1 else None
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
     t0 = time.perf_counter()
     probs = [Problem.from_deck(d) for d, _ in items]
     setup_s = time.perf_counter() - t0
@@ -308,7 +326,7 @@ def run_ensemble(args, torch):
 
     # ---- L1 after 50 steps: the batch in its mode against the batch in
     # FP64 (equal, mesh by mesh, to each mesh alone: tests/test_gpu_batch.py)
-    l1_50 = None
+    rows_50 = None
     if fp != fp_plain:
         ref = [p.copy() for p in probs]
         bm = BatchSolver(probs, fp_mode=fp)
@@ -319,7 +337,7 @@ def run_ensemble(args, torch):
         assert bf.run(max_steps=50)[0] == 0, bf.error.message
         bf.sync_to_host(0)
         bf.close()
-        l1_50 = l1_summary([l1s(a, b) for a, b in zip(probs, ref)])
+        rows_50 = [l1s(a, b) for a, b in zip(probs, ref)]
         del ref
         for i, p in enumerate(probs):
             restore(p, i)
@@ -337,7 +355,7 @@ def run_ensemble(args, torch):
     l0 = b.total_launches
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
+    barrier()
     with ClockSampler(torch.cuda.current_device()) as clk:
         e0.record(stream)
         ierr, status, nsteps = b.run_compacting(max_steps=K)
@@ -353,11 +371,11 @@ def run_ensemble(args, torch):
     b.sync_to_host(0)
     b.close()
     batch_final = [p.copy() for p in probs]
-    value = zc_b / (ms_b * 1e-3)
+    value, t_b, _ = job_rate(ms_b, zc_b, device=dev)
     # ---- e2e: batch set-up from the host arrays, the same run, full download
     for i, p in enumerate(probs):
         restore(p, i)
-    torch.cuda.synchronize()
+    barrier()
     t0 = time.perf_counter()
     be = BatchSolver(probs, fp_mode=fp)
     ierr, _, ne = be.run_compacting(max_steps=K)
@@ -367,7 +385,9 @@ def run_ensemble(args, torch):
     zc_e = sum(nel * p.timestep.nstep for nel, p in zip(nels, probs))
     h2d = sum(a.nbytes for p in probs for a in p.fields.values())
     be.close()
+    e2e_value, _, _ = job_rate((t1 - t0) * 1e3, zc_e, device=dev)
     # ---- plain: each mesh alone in FP64
+    barrier()
     ms_p, zc_p = 0.0, 0
     rows_end, dt_end = [], []
     for i, p in enumerate(probs):
@@ -393,13 +413,34 @@ def run_ensemble(args, torch):
         rows_end.append(l1s(batch_final[i], p))
         dt_end.append(abs(batch_final[i].timestep.time - ts.time) / max(ts.dt, 1e-300))
         s.close()
-    plain = zc_p / (ms_p * 1e-3)
+    plain, _, _ = job_rate(ms_p, zc_p, device=dev)
+    clocks = clk.summary()
+    parts = gather_to_root({"rows_end": rows_end, "dt_end": dt_end, "rows_50": rows_50,
+                            "steps": steps_b, "done": done, "launches": launches,
+                            "compactions": compactions, "nels": nels, "nsteps": nsteps,
+                            "h2d": h2d, "ne": ne, "setup_s": setup_s, "ms_p": ms_p,
+                            "clocks": clocks})
+    if rank != 0:
+        return None
+    rows_end = [r for q in parts for r in q["rows_end"]]
+    dt_end = [d for q in parts for d in q["dt_end"]]
+    l1_50 = (l1_summary([r for q in parts for r in q["rows_50"]])
+             if parts[0]["rows_50"] is not None else None)
+    steps_b = [k for q in parts for k in q["steps"]]
+    nels = [k for q in parts for k in q["nels"]]
+    done = sum(q["done"] for q in parts)
+    launches = sum(q["launches"] for q in parts)
+    nsteps = max(q["nsteps"] for q in parts)
+    ne = max(q["ne"] for q in parts)
+    h2d = sum(q["h2d"] for q in parts)
+    setup_s = max(q["setup_s"] for q in parts)
+    ms_p = max(q["ms_p"] for q in parts)
     hbm_peak, peak_kind = load_peaks()
     achieved = value * B_EUL / 1e9
     return {"metric": METRIC, "what": "batched ensemble vs the plain per-mesh FP64 GPU path",
-            "value": value, "unit": "zone-cycles/s", "n_gpus": 1, "steps": nsteps,
-            "warmup": W, "ms_per_step": ms_b / max(1, nsteps), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None,
+            "value": value, "unit": "zone-cycles/s", "n_gpus": world, "steps": nsteps,
+            "warmup": W, "ms_per_step": t_b / max(1, nsteps), "higher_is_better": True,
+            "scaling": "strong", "vs_baseline": None,
             "dtype": "f64" if fp != abi.FP_MIXED else "f64+f32 (mixed)", "data": "synthetic",
             "config": {"workload": "ensemble_%d_eulerian_sod_sedov" % n, "instances": n,
                        "seed": seed, "nel_total": sum(nels), "nel_min": min(nels),
@@ -413,10 +454,16 @@ def run_ensemble(args, torch):
                                "running when they hold less than half its elements "
                                "(BatchSolver.run_compacting)" % tg,
                        "compactions": [{"after_step": a, "meshes": m, "elements": e}
-                                       for a, m, e in compactions],
+                                       for a, m, e in parts[0]["compactions"]],
                        "autotune": {"graph_steps": tg, "node_block": tb,
                                     "ms_per_step": {"%d,%d" % k: v for k, v in tms.items()}},
-                       "setup_s": setup_s},
+                       "setup_s": setup_s,
+                       "shards": {"ranks": world,
+                                  "meshes": [len(q["nels"]) for q in parts],
+                                  "elements": [sum(q["nels"]) for q in parts],
+                                  "how": "replicas.shard: longest first by nx*ny*max(nx,ny), "
+                                         "no exchange; rank 0's compactions and autotune "
+                                         "shown"}},
             "plain_per_mesh": {"value": plain, "unit": "zone-cycles/s", "ms_total": ms_p,
                                "fp_mode": "exact" if fp_plain == abi.FP_EXACT else "fast",
                                "how": "each mesh alone through bl_run in FP64, the same run "
@@ -433,12 +480,12 @@ def run_ensemble(args, torch):
                          "peak_kind": peak_kind,
                          "note": "algorithmic bytes 1628 B per zone-cycle (Eulerian); the "
                                  "FP64 issue rate, not HBM, bounds the path"},
-            "e2e": {"value": zc_e / (t1 - t0), "unit": "zone-cycles/s",
+            "e2e": {"value": e2e_value, "unit": "zone-cycles/s",
                     "h2d_bytes_per_step": int(h2d / max(1, ne)),
                     "d2h_bytes_per_step": int(h2d / max(1, ne)),
                     "note": "bl_init_batch from the host arrays + %d steps + full download, "
                             "wall clock" % ne},
-            "gpu_launches": launches, "clocks": clk.summary()}
+            "gpu_launches": launches, "clocks": parts[0]["clocks"]}
 
 
 # Two-material Sod tubes for the learned closure (pressure and density of
@@ -886,10 +933,13 @@ def main():
     from bookleaf_f90_gb300 import build as blbuild
     from bookleaf_f90_gb300.replicas import job_rate
     blbuild.build()
-    if args.workload in ("ensemble", "closure", "closure-ensemble"):
+    if args.workload == "ensemble":
+        line = run_ensemble(args, torch, rank, world)   # every rank its share
         if rank == 0:
-            run = {"ensemble": run_ensemble, "closure": run_closure,
-                   "closure-ensemble": run_closure_ensemble}[args.workload]
+            print(json.dumps(line))
+    elif args.workload in ("closure", "closure-ensemble"):
+        if rank == 0:
+            run = {"closure": run_closure, "closure-ensemble": run_closure_ensemble}[args.workload]
             print(json.dumps(run(args, torch)))
         if world > 1:
             dist.destroy_process_group()

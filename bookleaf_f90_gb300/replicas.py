@@ -1,11 +1,42 @@
-"""Whole-job figures for independent replicas, one process per GPU.
+"""Whole-job figures for multi-GPU runs, one process per GPU.
 
-The hydro step does not shard without a halo exchange (the reference's
-typhon layer), so a multi-GPU run advances one independent replica of the
-mesh per rank and exchanges nothing on the data path.  The only collective
-is the end-of-run reduction here: the job's rate is the units all ranks
+The hydro step of one mesh does not shard without a halo exchange (the
+reference's typhon layer), so a multi-GPU run of one mesh advances an
+independent replica per rank.  A batch of independent meshes does shard:
+each rank takes its share of the meshes (``shard``) and runs them alone.
+Neither exchanges anything on the data path.  The only collectives are
+the end-of-run reductions here: the job's rate is the units all ranks
 processed divided by the slowest rank's time.
 """
+
+
+def shard(weights, world, rank):
+    """The indices of the items rank ``rank`` of ``world`` takes: the
+    longest-processing-time rule (items by decreasing weight, each to the
+    rank with the least weight so far, the lowest rank on ties), so that
+    the ranks' loads differ by at most the largest item.  Deterministic:
+    every rank computes the same assignment without communicating.  Each
+    rank's indices come back in increasing order."""
+    if world <= 1:
+        return list(range(len(weights)))
+    load = [0.0] * world
+    owner = [0] * len(weights)
+    for i in sorted(range(len(weights)), key=lambda i: (-float(weights[i]), i)):
+        r = min(range(world), key=lambda r: (load[r], r))
+        owner[i] = r
+        load[r] += float(weights[i])
+    return [i for i in range(len(weights)) if owner[i] == rank]
+
+
+def gather_to_root(obj):
+    """[every rank's obj] on rank 0 (None elsewhere); [obj] without a
+    group."""
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [obj]
+    out = [None] * dist.get_world_size() if dist.get_rank() == 0 else None
+    dist.gather_object(obj, out, dst=0)
+    return out
 
 
 def job_rate(local_ms, local_units, device=None):
