@@ -933,12 +933,12 @@ def main():
     from bookleaf_f90_gb300 import build as blbuild
     from bookleaf_f90_gb300.replicas import job_rate
     blbuild.build()
-    if args.workload == "ensemble":
-        line = run_ensemble(args, torch, rank, world)   # every rank its share
-        if rank == 0:
-            print(json.dumps(line))
-    elif args.workload in ("closure", "closure-ensemble"):
-        if rank == 0:
+    if args.workload in ("ensemble", "closure", "closure-ensemble"):
+        if args.workload == "ensemble":
+            line = run_ensemble(args, torch, rank, world)   # every rank its share
+            if rank == 0:
+                print(json.dumps(line))
+        elif rank == 0:
             run = {"closure": run_closure, "closure-ensemble": run_closure_ensemble}[args.workload]
             print(json.dumps(run(args, torch)))
         if world > 1:
