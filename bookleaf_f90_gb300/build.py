@@ -69,6 +69,7 @@ def build(force=False, verbose=False, extra=()):
         (common + ["--fmad=false", "-DBL_NS=exact", "-c", os.path.join(CSRC, "bl_kernels.cu"),
                    "-o", os.path.join(BUILD, "k_exact.o")]),
         (common + ["--fmad=true", "-DBL_NS=mixed", "-DBL_FAST_ALGEBRA=1", "-DBL_MIXED=1",
+                   "-DBL_GETDT_SPLIT=1",
                    "-ftz=true", "-prec-div=false", "-prec-sqrt=false", "-c",
                    os.path.join(CSRC, "bl_kernels.cu"), "-o", os.path.join(BUILD, "k_mixed.o")]),
         (common + ["-c", os.path.join(CSRC, "bl_capi.cu"), "-o", os.path.join(BUILD, "capi.o")]),

@@ -34,7 +34,8 @@ const bl::Launchers kFast = {bl::fast::getdt_blocks,          bl::fast::getdt_gr
                              bl::fast::launch_getdt_batch,     bl::fast::launch_lag_force_batch,
                              bl::fast::launch_lag_accel_batch, bl::fast::launch_lag_state_batch,
                              bl::fast::launch_ale_batch,       bl::fast::prepare_mix_closure,
-                             bl::fast::launch_mix_closure,     bl::fast::launch_mix_closure_batch};
+                             bl::fast::launch_mix_closure,     bl::fast::launch_mix_closure_batch,
+                             bl::fast::getdt_launches};
 const bl::Launchers kExact = {bl::exact::getdt_blocks,          bl::exact::getdt_grid,
                               bl::exact::launch_getdt,
                               bl::exact::launch_lag_force,       bl::exact::launch_lag_accel,
@@ -42,7 +43,8 @@ const bl::Launchers kExact = {bl::exact::getdt_blocks,          bl::exact::getdt
                               bl::exact::launch_getdt_batch,     bl::exact::launch_lag_force_batch,
                               bl::exact::launch_lag_accel_batch, bl::exact::launch_lag_state_batch,
                               bl::exact::launch_ale_batch,       bl::exact::prepare_mix_closure,
-                              bl::exact::launch_mix_closure,     bl::exact::launch_mix_closure_batch};
+                              bl::exact::launch_mix_closure,     bl::exact::launch_mix_closure_batch,
+                              bl::exact::getdt_launches};
 const bl::Launchers kMixed = {bl::mixed::getdt_blocks,          bl::mixed::getdt_grid,
                               bl::mixed::launch_getdt,
                               bl::mixed::launch_lag_force,       bl::mixed::launch_lag_accel,
@@ -50,7 +52,8 @@ const bl::Launchers kMixed = {bl::mixed::getdt_blocks,          bl::mixed::getdt
                               bl::mixed::launch_getdt_batch,     bl::mixed::launch_lag_force_batch,
                               bl::mixed::launch_lag_accel_batch, bl::mixed::launch_lag_state_batch,
                               bl::mixed::launch_ale_batch,       bl::mixed::prepare_mix_closure,
-                              bl::mixed::launch_mix_closure,     bl::mixed::launch_mix_closure_batch};
+                              bl::mixed::launch_mix_closure,     bl::mixed::launch_mix_closure_batch,
+                              bl::mixed::getdt_launches};
 
 // batches (defined with bl_init_batch below)
 void batch_copy(bl_ctx* x, int id, bool to_mesh);
@@ -714,7 +717,7 @@ int bl_getdt(bl_ctx* x, bl_timestep* ts, bl_error* e) {
     return BL_FAILURE;
   }
   header_from_ts(x, ts, 0);
-  x->launches += bl::kLaunchesGetdt;
+  x->launches += x->L.getdt_launches(x->C);
   int rc = run_call(x, kCallGetdt, e, "bl_getdt");
   if (rc != BL_SUCCESS) return rc;
   x->cs2_is_v = true;
@@ -832,7 +835,7 @@ int bl_run(bl_ctx* x, bl_timestep* ts, int max_steps, bl_step_record* history, i
   header_from_ts(x, ts, 1);
   // step limit: getdt stops once nrecord reaches it (DevStep.nrecord counts)
   int launched = 0;
-  const int per_step = bl::kLaunchesGetdt + bl::launches_lagstep(x->F) + (with_ale ? bl::kLaunchesAle : 0);
+  const int per_step = x->L.getdt_launches(x->C) + bl::launches_lagstep(x->F) + (with_ale ? bl::kLaunchesAle : 0);
   int done = 0;
   while (true) {
     const int remaining = max_steps - done;
@@ -935,7 +938,7 @@ int bl_time_step_kernels(bl_ctx* x, bl_timestep* ts, int nstep, double* ms, int 
     x->L.mix_closure(x->F, x->C, x->stream);
     cudaEventRecord(ev[4 * k + 4], x->stream);
   }
-  x->launches += (long long)nstep * (bl::kLaunchesGetdt + bl::launches_lagstep(x->F));
+  x->launches += (long long)nstep * (x->L.getdt_launches(x->C) + bl::launches_lagstep(x->F));
   r = cudaEventSynchronize(ev[4 * nstep]);
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
   for (int k = 0; k < nstep && r == cudaSuccess; k++)
@@ -1528,7 +1531,7 @@ int bl_run_batch(bl_ctx* x, bl_timestep* ts, int max_steps, int* status, int* ns
     x->b_gsteps = G;
     x->b_ndblock = F.nd_block;
   }
-  const int per_step = bl::kLaunchesGetdt + bl::launches_lagstep(x->F) + (with_ale ? bl::kLaunchesAle : 0);
+  const int per_step = x->L.getdt_launches(x->C) + bl::launches_lagstep(x->F) + (with_ale ? bl::kLaunchesAle : 0);
   int done = 0;
   while (done < max_steps) {
     const int k = std::min(G, max_steps - done);

@@ -29,6 +29,7 @@ namespace bl {
   int prepare_mix_closure();                                                       \
   void launch_mix_closure(const DevFields& F, const DevCfg& C, cudaStream_t s);    \
   void launch_mix_closure_batch(const DevFields& F, const DevCfg& C, cudaStream_t s);\
+  int getdt_launches(const DevCfg& C);                                             \
   }
 
 BL_DECLARE_LAUNCHERS(fast)
@@ -53,10 +54,12 @@ struct Launchers {
   int (*mix_prepare)();
   void (*mix_closure)(const DevFields&, const DevCfg&, cudaStream_t);
   void (*mix_closure_b)(const DevFields&, const DevCfg&, cudaStream_t);
+  // kernels one getdt launcher call launches (for bl_kernel_launches)
+  int (*getdt_launches)(const DevCfg&);
 };
 
-// Kernels launched by one call of each launcher (for bl_kernel_launches).
-constexpr int kLaunchesGetdt = 1;
+// Kernels launched by one call of each launcher (for bl_kernel_launches;
+// getdt's: Launchers::getdt_launches).
 constexpr int kLaunchesLagstep = 3;
 constexpr int kLaunchesAle = 4;
 // the lagstep launcher's count with the learned closure in it

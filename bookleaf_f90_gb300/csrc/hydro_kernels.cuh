@@ -73,6 +73,15 @@ static __device__ __noinline__ double dsqrt_call(double x) { return dsqrt_rn(x);
 #ifndef BL_GETDT_MINB
 #define BL_GETDT_MINB 7
 #endif
+// The fast build's k_getdt as two kernels (BL_GETDT_SPLIT): the edge
+// viscosity, then the dt scans and reduction.  Measured on Sedov 512x512:
+// the same step time in FP64 (293.6-294.0 against 293.6-293.8 us), 4-5 %
+// faster in the demoted form (k_getdt 62.1 against 68.7-71.0 us; 205.1
+// against 215.0 us per step), which is latency-bound and whose halves run
+// without spills; the build enables it for the demoted form only.
+#ifndef BL_GETDT_SPLIT
+#define BL_GETDT_SPLIT 0
+#endif
 // The fast build may also use exact algebraic identities that can change
 // only the sign of a zero (negation symmetry of opposite corners); the
 // exact build evaluates every expression as written.
@@ -849,7 +858,11 @@ __device__ __forceinline__ lr nb_ratio(const FaceQ& f, lr ddx, lr ddy, lr ddu, l
 // generated meshes elements are numbered along mesh lines, so the face
 // across face 2 and the two limiter neighbours of side 0 are the adjacent
 // elements and take the shared path.
-template <int BS, bool BATCH>
+// PART 0 is the whole kernel; with BL_GETDT_SPLIT the launch runs PART 1,
+// the edge viscosity (elvisc and the corner forces), then PART 2, which
+// reads elvisc back for the CFL and divergence candidates and the dt
+// reduction (the same blocks over the same elements in both).
+template <int BS, bool BATCH, int PART = 0>
 __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg C) {
   // the mesh of this block: the context's, or in a batch the block's own
   // (its blocks [blk0, blk0 + nblk), elements [el0, el1))
@@ -901,7 +914,7 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
       v[j] = F.ndv[n[j]];
     }
   }
-  if (!C.ztq) {
+  if (PART != 2 && !C.ztq) {
     if (inmesh) {
       const FaceQ f0 = face_q(to_lr(u[1] - u[0]), to_lr(v[1] - v[0]), to_lr(x[1] - x[0]),
                               to_lr(y[1] - y[0]), zl);
@@ -931,7 +944,7 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
   if (own) {
     const double rho0 = F.rho[iel];
     double visc = 0.0;
-    if (!C.ztq) {
+    if (PART != 2 && !C.ztq) {
       // hydro_kn_initeviscosity / limiteviscosity / geteviscosity
       // (hydro_kn_edgeviscosity.f90:30-282), face by face in the reference's
       // order 3, 1, 0, 2 (the faces of side s are (s+3)&3 and s+1)
@@ -1074,9 +1087,9 @@ __global__ void __launch_bounds__(BS, BL_GETDT_MINB) k_getdt(DevFields F, DevCfg
     } else {
       visc = F.visc[iel];
     }
-    getdt_tail(F, C, iel, x, y, u, v, visc, cflv, cfli, divv, divi);
+    if (PART != 1) getdt_tail(F, C, iel, x, y, u, v, visc, cflv, cfli, divv, divi);
   }
-  getdt_finish<BS, BATCH>(F, C, S, cflv, cfli, divv, divi, blk0, nblk, el0, I);
+  if (PART != 1) getdt_finish<BS, BATCH>(F, C, S, cflv, cfli, divv, divi, blk0, nblk, el0, I);
 }
 
 template <int BS>
@@ -1673,8 +1686,21 @@ int getdt_blocks(int nel) {
 // spread of finishing times is a spread of their speeds, not of their work)
 int getdt_grid(int nel) { return getdt_blocks(nel); }
 
+int getdt_launches(const DevCfg& C) {
+#if BL_FAST_ALGEBRA && BL_GETDT_SPLIT
+  return C.ztq ? 1 : 2;
+#else
+  (void)C;
+  return 1;
+#endif
+}
 void launch_getdt(const DevFields& F, const DevCfg& C, cudaStream_t s) {
+#if BL_FAST_ALGEBRA && BL_GETDT_SPLIT
+  if (!C.ztq) k_getdt<BS_DT, false, 1><<<getdt_grid(F.nel), BS_DT, 0, s>>>(F, C);
+  k_getdt<BS_DT, false, 2><<<getdt_grid(F.nel), BS_DT, 0, s>>>(F, C);
+#else
   k_getdt<BS_DT, false><<<getdt_grid(F.nel), BS_DT, 0, s>>>(F, C);
+#endif
 }
 void launch_lag_force(const DevFields& F, const DevCfg& C, cudaStream_t s) {
   k_lag_force<BS_EL, false><<<(F.nel + BS_EL - 1) / BS_EL, BS_EL, 0, s>>>(F, C);
@@ -1707,7 +1733,12 @@ void launch_mix_closure_batch(const DevFields& F, const DevCfg& C, cudaStream_t 
 // a batch of meshes: k_getdt over each mesh's own blocks, the rest over all
 // elements or nodes, each reading the step header of its mesh
 void launch_getdt_batch(const DevFields& F, const DevCfg& C, cudaStream_t s) {
+#if BL_FAST_ALGEBRA && BL_GETDT_SPLIT
+  if (!C.ztq) k_getdt<BS_DT, true, 1><<<F.nblk_batch, BS_DT, 0, s>>>(F, C);
+  k_getdt<BS_DT, true, 2><<<F.nblk_batch, BS_DT, 0, s>>>(F, C);
+#else
   k_getdt<BS_DT, true><<<F.nblk_batch, BS_DT, 0, s>>>(F, C);
+#endif
 }
 void launch_lag_force_batch(const DevFields& F, const DevCfg& C, cudaStream_t s) {
   k_lag_force<BS_EL, true><<<(F.nel + BS_EL - 1) / BS_EL, BS_EL, 0, s>>>(F, C);
