@@ -16,12 +16,27 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 from bookleaf_f90_gb300 import abi, configs  # noqa: E402
 
+
+def _deck(name):
+    with open(os.path.join(HERE, "decks", name)) as f:
+        return f.read()
+
+
 CASES = {
     "sod_lag_40x4": (configs.sod(40, 4), 60),
     "sedov_lag_24": (configs.sedov(24), 60),
     "noh_lag_24": (configs.noh(24), 40),
     "noh_eul_24": (configs.noh(24, eulerian=True), 40),
     "sod_mm_20x4": (configs.sod_multimaterial(20, 4), 40),
+    # the other equations of state, the hourglass and sub-zonal pressure
+    # forces of the benchmark's settings, the polar mesh of ARC sides, and
+    # one of the reference's own control files
+    "eos_tait_40x4": (configs.eos_tube("tait", 40, 4), 40),
+    "eos_jwl_40x4": (configs.eos_tube("jwl", 40, 4), 40),
+    "eos_void_40x4": (configs.eos_tube("void", 40, 4), 40),
+    "sedov_hg_sp_24": (configs.sedov(24, kappa=0.01, pmerit=0.1), 60),
+    "noh_polar_20x8": (configs.noh_polar(20, 8), 40),
+    "deck_sod_mm_lag_small": (_deck("sod_mm_lag_small"), 20),
 }
 
 
